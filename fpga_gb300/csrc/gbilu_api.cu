@@ -1,0 +1,833 @@
+// C ABI of libgbilu.so (declared in include/gbilu.h): handle lifetime,
+// device memory, the BiCGSTAB launch sequence, its CUDA graph (a device-side
+// while loop), iterative refinement for the mixed mode and the adjoint.
+#include "gbilu.h"
+#include "gbilu_host.hpp"
+#include "gbilu_kernels.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace gbilu {
+namespace {
+
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t alloc(size_t count) {
+    n = count;
+    return cudaMalloc(&p, std::max<size_t>(count, 1) * sizeof(T));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// device copy of one sliced matrix
+struct DevMat {
+  DevBuf<int> off, col;
+  DevBuf<double> v64;
+  DevBuf<float> v32;
+  void release() { off.release(); col.release(); v64.release(); v32.release(); }
+};
+
+// the nine work vectors of one BiCGSTAB run
+template <typename T> struct Vecs {
+  DevBuf<T> x, r, rt, p, ph, v, s, sh, t;
+  cudaError_t alloc(size_t n) {
+    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t}) {
+      cudaError_t e = b->alloc(n);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  void release() {
+    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t}) b->release();
+  }
+};
+
+// Everything one BiCGSTAB run reads: operator, preconditioner and vectors.
+template <typename V, typename T> struct Ops {
+  bool transpose;
+  const int *offA, *colA; const V *valA;     // A or A^T
+  const int *off1, *col1; const V *val1;     // first sweep: L or U^T
+  const int *off2, *col2; const V *val2;     // second sweep: U or L^T
+  const V *dmat;                             // Dinv or Dinv^T (sliced)
+  Vecs<T> *vec;
+};
+
+}  // namespace
+
+struct Handle {
+  gbilu_options opt{};
+  std::string err;
+  Analysis an;
+  bool analyzed = false, factored = false;
+  std::vector<double> pvals, lu, dinv;   // host: permuted A, factors
+  double analyze_ms = 0, factor_ms = 0;
+  // device
+  bool dev_ready = false;
+  int sm_count = 0;
+  cudaStream_t st = nullptr, cap = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  DevBuf<int2> srows;
+  DevBuf<int> perm, prowptr, pcol, psrc;
+  DevMat A, L, U, At, Ut, Lt;
+  DevBuf<double> dinv64, dinvT64;
+  DevBuf<float> dinv32, dinvT32;
+  Vecs<double> v64;
+  Vecs<float> v32;
+  DevBuf<double> b64, io64, io64b, partials, dA;
+  DevBuf<Ctl> ctl;                         // [0] main run, [1] refinement residual
+  Ctl *h_ctl = nullptr;                    // pinned mirror
+  bool with_t = false, with_32 = false;
+  cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][transpose]
+  int per_iter[2] = {0, 0};                // launches per iteration [transpose]
+  long long last_launches = 0;
+  size_t device_bytes = 0;
+
+  int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    if (opt.verbose) printf("ERROR: %s\n", buf);
+    return code;
+  }
+};
+
+namespace {
+
+#define CK(call)                                                                 \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess)                                                       \
+      return h->fail(GBILU_CUDA_ERROR, "%s: %s (%s:%d)", #call,                  \
+                     cudaGetErrorString(e_), __FILE__, __LINE__);                \
+  } while (0)
+
+int grid_for(const Handle *h, long long work) {
+  long long g = (work + kThreads - 1) / kThreads;
+  const long long cap = (long long)h->sm_count * 8;
+  return (int)std::max<long long>(1, std::min(g, cap));
+}
+
+// ---------------------------------------------------------------------------
+// launch sequences
+// ---------------------------------------------------------------------------
+
+template <typename V, typename T, bool D>
+void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, const V *val,
+                 const V *dmat, int c, const T *src, const T *nbr, T *dst, int &launches) {
+  const Analysis &an = h->an;
+  const int row0 = an.color_ptr[c], nrows = an.color_ptr[c + 1] - row0;
+  if (nrows <= 0) return;
+  k_sweep<V, T, D><<<(nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+      h->ctl.p, row0, nrows, an.slice_color_ptr[c], off, col, val, dmat, src, nbr, dst);
+  ++launches;
+}
+
+// hat = M^-1 src (forward) or M^-T src (transpose). In the forward case with
+// two or more colors, hat must already hold src on color 0's unknowns.
+template <typename V, typename T>
+void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *hat,
+                int &launches) {
+  const int C = h->an.ncolors;
+  if (!o.transpose) {
+    if (C == 1) {
+      sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, 0, src, hat, hat, launches);
+      return;
+    }
+    for (int c = 1; c < C; ++c) {
+      if (c == C - 1)   // the last color has no U blocks: fuse its D^-1
+        sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
+      else
+        sweep_color<V, T, false>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
+    }
+    for (int c = C - 2; c >= 0; --c)
+      sweep_color<V, T, true>(h, s, o.off2, o.col2, o.val2, o.dmat, c, hat, hat, hat, launches);
+  } else {
+    // U^T w = src forward over colors (diagonal blocks U_ii^T), then
+    // L^T z = w backward (unit diagonal); the last color's L^T rows are empty
+    for (int c = 0; c < C; ++c)
+      sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
+    for (int c = C - 2; c >= 0; --c)
+      sweep_color<V, T, false>(h, s, o.off2, o.col2, o.val2, o.dmat, c, hat, hat, hat, launches);
+  }
+}
+
+template <typename V, typename T, int MODE>
+void spmv(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *x, T *y, const T *w,
+          int &launches) {
+  const int S = h->an.S;
+  k_spmv<V, T, MODE><<<(S + kWarps - 1) / kWarps, kThreads, 0, s>>>(
+      h->ctl.p, S, h->srows.p, o.offA, o.colA, o.valA, x, y, w, h->partials.p);
+  ++launches;
+}
+
+// unknowns of color 0 that the producers copy into the preconditioned vector
+int first_color_unknowns(const Handle *h, bool transpose) {
+  if (transpose || h->an.ncolors < 2) return 0;
+  return 3 * h->an.color_ptr[1];
+}
+
+// One full BiCGSTAB iteration (both halves, PROGRAM steps 2-17).
+template <typename V, typename T>
+void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
+                       unsigned long long cond, int &launches) {
+  Vecs<T> &w = *o.vec;
+  const int n = 3 * h->an.nb, n0 = first_color_unknowns(h, o.transpose);
+  const int g = grid_for(h, n);
+  Ctl *c = h->ctl.p;
+  double *part = h->partials.p;
+  apply_prec(h, s, o, w.p.p, w.ph.p, launches);
+  spmv<V, T, SPMV_ALPHA>(h, s, o, w.ph.p, w.v.p, w.rt.p, launches);
+  k_update_s<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.s.p, w.sh.p, part);
+  apply_prec(h, s, o, w.s.p, w.sh.p, launches);
+  spmv<V, T, SPMV_OMEGA>(h, s, o, w.sh.p, w.t.p, w.s.p, launches);
+  k_update_r<T><<<g, kThreads, 0, s>>>(c, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p, w.rt.p,
+                                       w.r.p, part);
+  k_update_p<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.p.p, w.ph.p, cond);
+  launches += 3;
+}
+
+template <typename V, typename T>
+int build_graph(Handle *h, const Ops<V, T> &o, cudaGraphExec_t &exec, int &per_iter) {
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams params = {};
+  params.type = cudaGraphNodeTypeConditional;
+  params.conditional.handle = cond;
+  params.conditional.type = cudaGraphCondTypeWhile;
+  params.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &params));
+  cudaGraph_t body = params.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(h->cap, body, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  int launches = 0;
+  enqueue_iteration(h, h->cap, o, (unsigned long long)cond, launches);
+  cudaGraph_t captured = nullptr;
+  CK(cudaStreamEndCapture(h->cap, &captured));
+  CK(cudaGraphInstantiate(&exec, g, 0));
+  CK(cudaGraphDestroy(g));
+  per_iter = launches;
+  return GBILU_OK;
+}
+
+template <typename V, typename T> Ops<V, T> make_ops(Handle *h, bool transpose);
+
+template <> Ops<double, double> make_ops(Handle *h, bool t) {
+  Ops<double, double> o;
+  o.transpose = t;
+  DevMat &a = t ? h->At : h->A, &m1 = t ? h->Ut : h->L, &m2 = t ? h->Lt : h->U;
+  o.offA = a.off.p; o.colA = a.col.p; o.valA = a.v64.p;
+  o.off1 = m1.off.p; o.col1 = m1.col.p; o.val1 = m1.v64.p;
+  o.off2 = m2.off.p; o.col2 = m2.col.p; o.val2 = m2.v64.p;
+  o.dmat = t ? h->dinvT64.p : h->dinv64.p;
+  o.vec = &h->v64;
+  return o;
+}
+
+template <> Ops<float, float> make_ops(Handle *h, bool t) {
+  Ops<float, float> o;
+  o.transpose = t;
+  DevMat &a = t ? h->At : h->A, &m1 = t ? h->Ut : h->L, &m2 = t ? h->Lt : h->U;
+  o.offA = a.off.p; o.colA = a.col.p; o.valA = a.v32.p;
+  o.off1 = m1.off.p; o.col1 = m1.col.p; o.val1 = m1.v32.p;
+  o.off2 = m2.off.p; o.col2 = m2.col.p; o.val2 = m2.v32.p;
+  o.dmat = t ? h->dinvT32.p : h->dinv32.p;
+  o.vec = &h->v32;
+  return o;
+}
+
+// Runs the iteration loop of an already initialised Ctl (after the init
+// kernels), as a graph or host-driven, then the x fix-up.
+template <typename V, typename T>
+int run_loop(Handle *h, bool transpose, int maxit, long long &launches) {
+  Ops<V, T> o = make_ops<V, T>(h, transpose);
+  const int fp32 = sizeof(T) == 4 ? 1 : 0, ti = transpose ? 1 : 0;
+  const int n = 3 * h->an.nb;
+  if (h->opt.use_graph) {
+    if (!h->graph[fp32][ti]) {
+      int rc = build_graph(h, o, h->graph[fp32][ti], h->per_iter[ti]);
+      if (rc) return rc;
+    }
+    CK(cudaGraphLaunch(h->graph[fp32][ti], h->st));
+  } else {
+    // host-driven: enqueue two iterations, then look at the done flag
+    for (int it = 0; it <= maxit + 1; it += 2) {
+      int l = 0;
+      enqueue_iteration(h, h->st, o, 0ull, l);
+      enqueue_iteration(h, h->st, o, 0ull, l);
+      h->per_iter[ti] = l / 2;
+      launches += l;
+      CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      if (h->h_ctl->done) break;
+    }
+  }
+  k_finish_x<T><<<grid_for(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, o.vec->x.p, o.vec->ph.p);
+  launches += 1;
+  CK(cudaGetLastError());
+  return GBILU_OK;
+}
+
+void fill_result(const Handle *h, const Ctl &c, gbilu_result *res) {
+  res->status = c.status;
+  res->half_iters = c.status == ST_ALREADY || (c.status == ST_NONFINITE && c.half < 0) ? -1 : c.half;
+  res->iterations = res->half_iters / 2.0 + 0.5;
+  res->norm0 = c.norm0;
+  res->norm = c.norm;
+  res->relres = c.norm0 > 0 ? c.norm / c.norm0 : 0.0;
+  for (int i = 0; i < 4; ++i) res->norms[i] = c.norms[i];
+  res->last_norm_idx = c.last_norm_idx;
+  (void)h;
+}
+
+// ---------------------------------------------------------------------------
+// device set-up
+// ---------------------------------------------------------------------------
+
+int upload_mat(Handle *h, const SlicedMatrix &m, DevMat &d) {
+  CK(d.off.alloc(m.off.size()));
+  CK(d.col.alloc(m.col.size()));
+  CK(cudaMemcpy(d.off.p, m.off.data(), m.off.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d.col.p, m.col.data(), m.col.size() * sizeof(int), cudaMemcpyHostToDevice));
+  const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
+  CK(d.v64.alloc(nv));
+  if (h->with_32) CK(d.v32.alloc(nv));
+  h->device_bytes += (m.off.size() + m.col.size()) * sizeof(int) + nv * 8 + (h->with_32 ? nv * 4 : 0);
+  return GBILU_OK;
+}
+
+int upload_vals(Handle *h, const SlicedMatrix &m, const double *src, DevMat &d) {
+  const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
+  std::vector<double> tmp(nv);
+  fill_sliced<double>(m, src, tmp.data());
+  CK(cudaMemcpy(d.v64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  if (h->with_32) {
+    std::vector<float> t32(nv);
+    for (size_t i = 0; i < nv; ++i) t32[i] = (float)tmp[i];
+    CK(cudaMemcpy(d.v32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return GBILU_OK;
+}
+
+int upload_diag(Handle *h, bool transpose, DevBuf<double> &d64, DevBuf<float> &d32) {
+  const size_t nv = (size_t)h->an.S * 9 * kSliceRows;
+  std::vector<double> tmp(nv);
+  fill_sliced_diag<double>(h->an, h->dinv.data(), transpose, tmp.data());
+  CK(cudaMemcpy(d64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  if (h->with_32) {
+    std::vector<float> t32(nv);
+    for (size_t i = 0; i < nv; ++i) t32[i] = (float)tmp[i];
+    CK(cudaMemcpy(d32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return GBILU_OK;
+}
+
+void release_device(Handle *h) {
+  if (!h->dev_ready) return;
+  cudaSetDevice(h->opt.device);
+  for (auto &row : h->graph)
+    for (auto &g : row)
+      if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  for (DevMat *m : {&h->A, &h->L, &h->U, &h->At, &h->Ut, &h->Lt}) m->release();
+  h->srows.release(); h->perm.release(); h->prowptr.release(); h->pcol.release();
+  h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
+  h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
+  h->io64.release(); h->io64b.release(); h->partials.release(); h->dA.release();
+  h->ctl.release();
+  h->device_bytes = 0;
+}
+
+// Allocates the device side for the current analysis (structure only).
+int setup_device(Handle *h) {
+  if (h->opt.device < 0) return h->fail(GBILU_NO_DEVICE, "host-only handle has no device");
+  CK(cudaSetDevice(h->opt.device));
+  if (!h->st) {
+    CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&h->e0));
+    CK(cudaEventCreate(&h->e1));
+    CK(cudaMallocHost(&h->h_ctl, sizeof(Ctl)));
+    CK(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->opt.device));
+  }
+  release_device(h);
+  h->dev_ready = true;
+  const Analysis &an = h->an;
+  const size_t n = 3 * (size_t)an.nb;
+  h->with_t = true;
+  h->with_32 = h->opt.precision == GBILU_MIXED;
+  std::vector<int2> sr(an.S);
+  for (int s = 0; s < an.S; ++s) sr[s] = make_int2(an.slice_row0[s], an.slice_len[s]);
+  CK(h->srows.alloc(an.S));
+  CK(cudaMemcpy(h->srows.p, sr.data(), sr.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CK(h->perm.alloc(an.nb));
+  CK(cudaMemcpy(h->perm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->prowptr.alloc(an.nb + 1));
+  CK(cudaMemcpy(h->prowptr.p, an.prowptr.data(), (an.nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->pcol.alloc(an.nnzb));
+  CK(cudaMemcpy(h->pcol.p, an.pcolind.data(), an.nnzb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->psrc.alloc(an.nnzb));
+  CK(cudaMemcpy(h->psrc.p, an.psrc.data(), an.nnzb * sizeof(int), cudaMemcpyHostToDevice));
+  for (auto pr : {std::make_pair(&an.A, &h->A), std::make_pair(&an.L, &h->L),
+                  std::make_pair(&an.U, &h->U), std::make_pair(&an.At, &h->At),
+                  std::make_pair(&an.Ut, &h->Ut), std::make_pair(&an.Lt, &h->Lt)}) {
+    int rc = upload_mat(h, *pr.first, *pr.second);
+    if (rc) return rc;
+  }
+  const size_t nd = (size_t)an.S * 9 * kSliceRows;
+  CK(h->dinv64.alloc(nd));
+  CK(h->dinvT64.alloc(nd));
+  if (h->with_32) { CK(h->dinv32.alloc(nd)); CK(h->dinvT32.alloc(nd)); }
+  CK(h->v64.alloc(n));
+  if (h->with_32) CK(h->v32.alloc(n));
+  CK(h->b64.alloc(n));
+  CK(h->io64.alloc(n));
+  CK(h->io64b.alloc(n));
+  const size_t maxgrid = std::max<size_t>((size_t)h->sm_count * 8, (size_t)(an.S + kWarps - 1) / kWarps) + 1;
+  CK(h->partials.alloc(2 * maxgrid));
+  CK(h->ctl.alloc(2));
+  h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
+                     (size_t)an.nnzb * 8 + (size_t)an.nb * 8;
+  return GBILU_OK;
+}
+
+int check_solve_ready(Handle *h) {
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  if (!h->factored) return h->fail(GBILU_NOT_READY, "gbilu_factor has not been called");
+  if (h->opt.device < 0) return h->fail(GBILU_NO_DEVICE, "host-only handle cannot solve");
+  return GBILU_OK;
+}
+
+// FP64 BiCGSTAB on the permuted vectors: b in h->b64, x in v64.x.
+int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long long &launches) {
+  const int n = 3 * h->an.nb;
+  Ops<double, double> o = make_ops<double, double>(h, transpose);
+  Vecs<double> &w = h->v64;
+  const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
+  k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, tol, h->opt.absolute_tol, maxit, tmo);
+  int l = 1;
+  spmv<double, double, SPMV_RESID>(h, h->st, o, w.x.p, w.r.p, h->b64.p, l);
+  launches += l;
+  k_init_vectors<double><<<grid_for(h, n), kThreads, 0, h->st>>>(
+      h->ctl.p, n, first_color_unknowns(h, transpose), w.r.p, w.rt.p, w.p.p, w.ph.p);
+  launches += 1;
+  int rc = run_loop<double, double>(h, transpose, maxit, launches);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  out = *h->h_ctl;
+  return GBILU_OK;
+}
+
+// Mixed precision: FP32 inner BiCGSTAB inside FP64 iterative refinement.
+// b in h->b64, x in v64.x (FP64, permuted).
+int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *res,
+                Ctl &out, long long &launches) {
+  const int n = 3 * h->an.nb;
+  Ops<double, double> o64 = make_ops<double, double>(h, transpose);
+  Vecs<double> &w = h->v64;
+  Vecs<float> &f = h->v32;
+  Ctl *outer = h->ctl.p + 1;
+  const int g = grid_for(h, n);
+  auto residual = [&](double &nrm) -> int {
+    // r = b - A x in FP64 with the FP64 copy of A, ||r|| read back
+    k_ctl_init<<<1, 32, 0, h->st>>>(outer, 0.0, 1, 0, 0ull);
+    const int S = h->an.S;
+    k_spmv<double, double, SPMV_RESID><<<(S + kWarps - 1) / kWarps, kThreads, 0, h->st>>>(
+        outer, S, h->srows.p, o64.offA, o64.colA, o64.valA, w.x.p, w.r.p, h->b64.p, h->partials.p);
+    launches += 2;
+    CK(cudaMemcpyAsync(h->h_ctl, outer, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    nrm = h->h_ctl->norm0;
+    return GBILU_OK;
+  };
+  double nrm0 = 0, nrm = 0;
+  int rc = residual(nrm0);
+  if (rc) return rc;
+  nrm = nrm0;
+  memset(&out, 0, sizeof out);
+  out.norm0 = nrm0;
+  out.norms[0] = nrm0;
+  out.status = ST_MAXIT;
+  if (!std::isfinite(nrm0)) { out.status = ST_NONFINITE; out.half = -1; out.norm = nrm0; return GBILU_OK; }
+  const double bound = h->opt.absolute_tol ? tol : tol * nrm0;
+  if (!(nrm0 > (h->opt.absolute_tol ? tol : kAlreadySolved))) {
+    out.status = ST_ALREADY; out.half = -1; out.norm = nrm0;
+    return GBILU_OK;
+  }
+  const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
+  const int n0 = first_color_unknowns(h, transpose);
+  int outer_steps = 0, inner_half = 0;
+  while (nrm > bound && outer_steps < h->opt.max_outer) {
+    // right-hand side of the correction equation A d = r / ||r|| in FP32
+    // (staged in f.t, which the inner run overwrites only after reading it)
+    k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0 / nrm, w.r.p, f.t.p);
+    k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, h->opt.inner_tol, 0, h->opt.inner_maxit, tmo);
+    k_init_rhs<float><<<g, kThreads, 0, h->st>>>(h->ctl.p, n, n0, f.t.p, f.r.p, f.rt.p, f.p.p,
+                                                f.ph.p, f.x.p, h->partials.p);
+    launches += 3;
+    rc = run_loop<float, float>(h, transpose, h->opt.inner_maxit, launches);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const Ctl ic = *h->h_ctl;
+    inner_half += (ic.half >= 0 ? ic.half + 1 : 0);
+    ++outer_steps;
+    if (ic.status == ST_BREAKDOWN || ic.status == ST_NONFINITE) { out.status = ic.status; break; }
+    k_axpy_f2d<<<g, kThreads, 0, h->st>>>(n, nrm, f.x.p, w.x.p);
+    launches += 1;
+    rc = residual(nrm);
+    if (rc) return rc;
+    if (!std::isfinite(nrm)) { out.status = ST_NONFINITE; break; }
+    if (ic.status == ST_TIMEOUT) { out.status = ST_TIMEOUT; break; }
+  }
+  (void)maxit;
+  if (nrm <= bound) out.status = ST_OK;
+  out.norm = nrm;
+  out.half = inner_half - 1;
+  if (res) {
+    res->outer_iters = outer_steps;
+    res->inner_half_iters = inner_half;
+    res->true_relres = nrm0 > 0 ? nrm / nrm0 : 0.0;
+  }
+  out.norms[1] = nrm;
+  out.last_norm_idx = 1;
+  return GBILU_OK;
+}
+
+}  // namespace
+}  // namespace gbilu
+
+using namespace gbilu;
+
+extern "C" {
+
+int gbilu_default_options(gbilu_options *o) {
+  if (!o) return GBILU_BAD_INPUT;
+  memset(o, 0, sizeof *o);
+  o->precision = GBILU_FP64;
+  o->absolute_tol = 0;
+  o->device = 0;
+  o->use_graph = 1;
+  o->timeout_ms = 0.0;
+  o->inner_tol = 1e-4;
+  o->inner_maxit = 500;
+  o->max_outer = 30;
+  o->verbose = 0;
+  return GBILU_OK;
+}
+
+int gbilu_create(const gbilu_options *opt, void **handle) {
+  if (!handle) return GBILU_BAD_INPUT;
+  *handle = nullptr;
+  Handle *h = new (std::nothrow) Handle();
+  if (!h) return GBILU_BAD_INPUT;
+  if (opt) h->opt = *opt; else gbilu_default_options(&h->opt);
+  if (h->opt.precision != GBILU_FP64 && h->opt.precision != GBILU_MIXED) {
+    delete h;
+    return GBILU_BAD_INPUT;
+  }
+  *handle = h;
+  return GBILU_OK;
+}
+
+int gbilu_destroy(void *handle) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (h->st) {
+    cudaSetDevice(h->opt.device);
+    cudaStreamSynchronize(h->st);
+    release_device(h);
+    cudaStreamDestroy(h->st);
+    cudaStreamDestroy(h->cap);
+    cudaEventDestroy(h->e0);
+    cudaEventDestroy(h->e1);
+    cudaFreeHost(h->h_ctl);
+  }
+  delete h;
+  return GBILU_OK;
+}
+
+int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  auto t0 = std::chrono::steady_clock::now();
+  h->analyzed = h->factored = false;
+  std::string err = analyze(nb, rowptr, colind, h->an, true);
+  if (!err.empty()) return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: %s", err.c_str());
+  h->analyzed = true;
+  if (h->opt.device >= 0) {
+    int rc = setup_device(h);
+    if (rc) return rc;
+  }
+  h->analyze_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (h->opt.verbose)
+    printf("INFO: gbilu_analyze: nb=%d nnzb=%d colors=%d slices=%d (%.1f ms)\n", nb, h->an.nnzb,
+           h->an.ncolors, h->an.S, h->analyze_ms);
+  return GBILU_OK;
+}
+
+int gbilu_get_ordering(void *handle, int *ncolors, int *color, int *perm, int *color_ptr) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  if (ncolors) *ncolors = h->an.ncolors;
+  if (color) memcpy(color, h->an.color.data(), h->an.nb * sizeof(int));
+  if (perm) memcpy(perm, h->an.perm.data(), h->an.nb * sizeof(int));
+  if (color_ptr) memcpy(color_ptr, h->an.color_ptr.data(), (h->an.ncolors + 1) * sizeof(int));
+  return GBILU_OK;
+}
+
+int gbilu_factor(void *handle, const double *vals) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  if (!vals) return h->fail(GBILU_BAD_INPUT, "vals must not be NULL");
+  auto t0 = std::chrono::steady_clock::now();
+  h->factored = false;
+  const Analysis &an = h->an;
+  h->pvals.resize((size_t)an.nnzb * 9);
+  permute_values(an, vals, h->pvals.data());
+  h->lu = h->pvals;
+  h->dinv.assign((size_t)an.nb * 9, 0.0);
+  const int bad = bilu0(an, h->lu.data(), h->dinv.data());
+  if (bad >= 0)
+    return h->fail(GBILU_SINGULAR, "gbilu_factor: singular diagonal block in permuted row %d (input row %d)",
+                   bad, an.perm[bad]);
+  if (h->opt.device >= 0) {
+    CK(cudaSetDevice(h->opt.device));
+    int rc;
+    if ((rc = upload_vals(h, an.A, h->pvals.data(), h->A))) return rc;
+    if ((rc = upload_vals(h, an.L, h->lu.data(), h->L))) return rc;
+    if ((rc = upload_vals(h, an.U, h->lu.data(), h->U))) return rc;
+    if ((rc = upload_vals(h, an.At, h->pvals.data(), h->At))) return rc;
+    if ((rc = upload_vals(h, an.Ut, h->lu.data(), h->Ut))) return rc;
+    if ((rc = upload_vals(h, an.Lt, h->lu.data(), h->Lt))) return rc;
+    if ((rc = upload_diag(h, false, h->dinv64, h->dinv32))) return rc;
+    if ((rc = upload_diag(h, true, h->dinvT64, h->dinvT32))) return rc;
+  }
+  h->factored = true;
+  h->factor_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return GBILU_OK;
+}
+
+int gbilu_get_factors(void *handle, double *lu, double *dinv) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!h->factored) return h->fail(GBILU_NOT_READY, "gbilu_factor has not been called");
+  if (lu) memcpy(lu, h->lu.data(), h->lu.size() * sizeof(double));
+  if (dinv) memcpy(dinv, h->dinv.data(), h->dinv.size() * sizeof(double));
+  return GBILU_OK;
+}
+
+static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, bool transpose,
+                      double tol, int maxit, gbilu_result *res) {
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  if (!b || !x) return h->fail(GBILU_BAD_INPUT, "b and x must not be NULL");
+  if (maxit < 0) return h->fail(GBILU_BAD_INPUT, "maxit must be >= 0");
+  if (!(tol >= 0.0)) return h->fail(GBILU_BAD_INPUT, "tol must be >= 0");
+  auto t0 = std::chrono::steady_clock::now();
+  CK(cudaSetDevice(h->opt.device));
+  const int nb = h->an.nb, n = 3 * nb;
+  const int g = grid_for(h, n);
+  long long launches = 0;
+  CK(cudaEventRecord(h->e0, h->st));
+  const double *db = b;
+  const double *dx = x;
+  if (!device_ptrs) {
+    CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    db = h->io64.p;
+    dx = h->io64b.p;
+  }
+  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, db, h->b64.p, 1.0);
+  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
+  launches += 2;
+  Ctl c;
+  gbilu_result tmp;
+  memset(&tmp, 0, sizeof tmp);
+  gbilu_result *r = res ? res : &tmp;
+  memset(r, 0, sizeof *r);
+  if (h->opt.precision == GBILU_MIXED)
+    rc = solve_mixed(h, transpose, tol, maxit, r, c, launches);
+  else
+    rc = solve64(h, transpose, tol, maxit, c, launches);
+  if (rc) return rc;
+  double *out = device_ptrs ? x : h->io64b.p;
+  if (c.status != ST_ALREADY) {
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p, out);
+    launches += 1;
+  }
+  CK(cudaEventRecord(h->e1, h->st));
+  if (!device_ptrs && c.status != ST_ALREADY)
+    CK(cudaMemcpyAsync(x, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaGetLastError());
+  const int outer = r->outer_iters, inner = r->inner_half_iters;
+  const double tr = r->true_relres;
+  fill_result(h, c, r);
+  r->outer_iters = outer;
+  r->inner_half_iters = inner;
+  r->true_relres = h->opt.precision == GBILU_MIXED ? tr : r->relres;
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->e0, h->e1));
+  r->device_ms = ms;
+  r->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  h->last_launches = launches;
+  if (h->opt.verbose)
+    printf("INFO: gbilu_solve: status=%d half_iters=%d relres=%.3e device %.3f ms\n", r->status,
+           r->half_iters, r->relres, r->device_ms);
+  return GBILU_OK;
+}
+
+int gbilu_solve(void *handle, const double *b, double *x, double tol, int maxit, gbilu_result *res) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  return solve_impl(h, b, x, false, false, tol, maxit, res);
+}
+
+int gbilu_solve_device(void *handle, const double *d_b, double *d_x, double tol, int maxit,
+                       gbilu_result *res) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  return solve_impl(h, d_b, d_x, true, false, tol, maxit, res);
+}
+
+int gbilu_apply_spmv(void *handle, const double *x, double *y, int transpose) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  if (!x || !y) return h->fail(GBILU_BAD_INPUT, "x and y must not be NULL");
+  CK(cudaSetDevice(h->opt.device));
+  const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
+  Ops<double, double> o = make_ops<double, double>(h, transpose != 0);
+  Vecs<double> &w = h->v64;
+  int launches = 0;
+  CK(cudaMemcpyAsync(h->io64.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64.p, w.p.p, 1.0);
+  spmv<double, double, SPMV_PLAIN>(h, h->st, o, w.p.p, w.v.p, nullptr, launches);
+  k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, w.v.p, h->io64b.p);
+  CK(cudaMemcpyAsync(y, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaGetLastError());
+  h->last_launches = launches + 2;
+  return GBILU_OK;
+}
+
+int gbilu_apply_ilu(void *handle, const double *p, double *z, int transpose) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  if (!p || !z) return h->fail(GBILU_BAD_INPUT, "p and z must not be NULL");
+  CK(cudaSetDevice(h->opt.device));
+  const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
+  const bool t = transpose != 0;
+  Ops<double, double> o = make_ops<double, double>(h, t);
+  Vecs<double> &w = h->v64;
+  int launches = 0;
+  k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
+  CK(cudaMemcpyAsync(h->io64.p, p, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64.p, w.p.p, 1.0);
+  const int n0 = first_color_unknowns(h, t);
+  if (n0) CK(cudaMemcpyAsync(w.ph.p, w.p.p, n0 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  apply_prec(h, h->st, o, w.p.p, w.ph.p, launches);
+  k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, w.ph.p, h->io64b.p);
+  CK(cudaMemcpyAsync(z, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaGetLastError());
+  h->last_launches = launches + 3;
+  return GBILU_OK;
+}
+
+int gbilu_adjoint(void *handle, const double *g_in, const double *x, double *lambda, double *dA,
+                  double tol, int maxit, gbilu_result *res) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!g_in || !x || !lambda) return h->fail(GBILU_BAD_INPUT, "g, x and lambda must not be NULL");
+  // lambda = A^-T g: the transposed solve, x0 = 0
+  std::vector<double> zero(3 * (size_t)(h->analyzed ? h->an.nb : 0), 0.0);
+  memcpy(lambda, zero.data(), zero.size() * sizeof(double));
+  int rc = solve_impl(h, g_in, lambda, false, true, tol, maxit, res);
+  if (rc) return rc;
+  if (dA) {
+    const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
+    CK(h->dA.n == (size_t)h->an.nnzb * 9 ? cudaSuccess : (h->dA.release(), h->dA.alloc((size_t)h->an.nnzb * 9)));
+    // lambda and x in the permuted numbering
+    CK(cudaMemcpyAsync(h->io64.p, lambda, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64.p, h->v64.r.p, 1.0);
+    CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64b.p, h->v64.s.p, 1.0);
+    k_grad_a<<<grid_for(h, nb), kThreads, 0, h->st>>>(nb, h->prowptr.p, h->pcol.p, h->psrc.p,
+                                                      h->v64.r.p, h->v64.s.p, h->dA.p);
+    CK(cudaMemcpyAsync(dA, h->dA.p, (size_t)h->an.nnzb * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+  }
+  return GBILU_OK;
+}
+
+int gbilu_get_stats(void *handle, gbilu_stats *s) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h || !s) return GBILU_BAD_INPUT;
+  memset(s, 0, sizeof *s);
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  const Analysis &an = h->an;
+  s->nb = an.nb;
+  s->nnzb = an.nnzb;
+  s->ncolors = an.ncolors;
+  s->nnzb_lower = an.nnzb_l;
+  s->nnzb_upper = an.nnzb_u;
+  s->slices = an.S;
+  s->slots_a = an.A.slots();
+  s->slots_l = an.L.slots();
+  s->slots_u = an.U.slots();
+  s->device_bytes = (long long)h->device_bytes;
+  s->launches_per_iter = h->per_iter[0];
+  s->last_launches = h->last_launches;
+  s->factor_ms = h->factor_ms;
+  s->analyze_ms = h->analyze_ms;
+  return GBILU_OK;
+}
+
+const char *gbilu_status_string(int s) {
+  switch (s) {
+    case GBILU_OK: return "ok";
+    case GBILU_MAXIT: return "maximum iterations reached";
+    case GBILU_ALREADY_CONVERGED: return "initial residual already below the bound";
+    case GBILU_BREAKDOWN: return "BiCGSTAB breakdown";
+    case GBILU_NONFINITE: return "non-finite residual";
+    case GBILU_TIMEOUT: return "device time budget exceeded";
+    case GBILU_BAD_INPUT: return "bad input";
+    case GBILU_SINGULAR: return "singular diagonal block";
+    case GBILU_CUDA_ERROR: return "CUDA error";
+    case GBILU_NOT_READY: return "call order";
+    case GBILU_NO_DEVICE: return "host-only handle";
+    default: return "unknown status";
+  }
+}
+
+const char *gbilu_last_error(void *handle) {
+  Handle *h = static_cast<Handle *>(handle);
+  return h ? h->err.c_str() : "null handle";
+}
+
+}  // extern "C"

@@ -1,0 +1,296 @@
+// Host-side analysis, block ILU0 and sliced layout (see gbilu_host.hpp).
+#include "gbilu_host.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace gbilu {
+
+int color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
+  // First-fit greedy in natural order: a row takes the smallest color that no
+  // already colored neighbour holds. stamp[c] == i+1 marks color c as taken
+  // for row i.
+  std::vector<int> stamp(static_cast<size_t>(nb) + 1, 0);
+  int ncolors = 0;
+  std::fill(color, color + nb, -1);
+  for (int i = 0; i < nb; ++i) {
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = colind[k];
+      if (j != i && color[j] >= 0) stamp[color[j]] = i + 1;
+    }
+    int c = 0;
+    while (stamp[c] == i + 1) ++c;
+    color[i] = c;
+    ncolors = std::max(ncolors, c + 1);
+  }
+  return ncolors;
+}
+
+std::string check_pattern(int nb, const int *rowptr, const int *colind) {
+  if (nb <= 0) return "nb must be positive";
+  if (!rowptr || !colind) return "rowptr/colind must not be NULL";
+  if (rowptr[0] != 0) return "rowptr[0] must be 0";
+  for (int i = 0; i < nb; ++i) {
+    if (rowptr[i + 1] < rowptr[i]) return "rowptr must be non-decreasing";
+    bool diag = false;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = colind[k];
+      if (j < 0 || j >= nb) return "column index out of range in row " + std::to_string(i);
+      if (k > rowptr[i] && colind[k - 1] >= j)
+        return "columns must be sorted and unique in row " + std::to_string(i);
+      diag |= (j == i);
+    }
+    if (!diag) return "missing diagonal block in row " + std::to_string(i);
+  }
+  return "";
+}
+
+namespace {
+
+struct Csr {
+  std::vector<int> rowptr, col, src;
+};
+
+// Builds the sliced layout of a CSR matrix (rows in permuted numbering).
+void slice_matrix(const Analysis &an, const Csr &m, bool transpose_blocks,
+                  SlicedMatrix &out) {
+  out.transpose_blocks = transpose_blocks;
+  out.off.assign(static_cast<size_t>(an.S) + 1, 0);
+  for (int s = 0; s < an.S; ++s) {
+    int w = 0;
+    for (int l = 0; l < an.slice_len[s]; ++l) {
+      const int r = an.slice_row0[s] + l;
+      w = std::max(w, m.rowptr[r + 1] - m.rowptr[r]);
+    }
+    out.off[s + 1] = out.off[s] + w;
+  }
+  const size_t n = static_cast<size_t>(out.off[an.S]) * kSliceRows;
+  out.col.assign(n, -1);
+  out.vsrc.assign(n, -1);
+  for (int s = 0; s < an.S; ++s) {
+    for (int l = 0; l < an.slice_len[s]; ++l) {
+      const int r = an.slice_row0[s] + l;
+      for (int k = m.rowptr[r]; k < m.rowptr[r + 1]; ++k) {
+        const size_t slot = static_cast<size_t>(out.off[s]) + (k - m.rowptr[r]);
+        out.col[slot * kSliceRows + l] = m.col[k];
+        out.vsrc[slot * kSliceRows + l] = m.src[k];
+      }
+    }
+  }
+}
+
+// Transpose of a CSR pattern selection: entries (i -> j, src) become (j -> i).
+Csr transpose_csr(int nb, const Csr &m) {
+  Csr t;
+  t.rowptr.assign(static_cast<size_t>(nb) + 1, 0);
+  for (int c : m.col) t.rowptr[c + 1]++;
+  for (int i = 0; i < nb; ++i) t.rowptr[i + 1] += t.rowptr[i];
+  t.col.resize(m.col.size());
+  t.src.resize(m.col.size());
+  std::vector<int> fill(t.rowptr.begin(), t.rowptr.end() - 1);
+  for (int i = 0; i < nb; ++i)            // rows ascending -> columns sorted
+    for (int k = m.rowptr[i]; k < m.rowptr[i + 1]; ++k) {
+      const int p = fill[m.col[k]]++;
+      t.col[p] = i;
+      t.src[p] = m.src[k];
+    }
+  return t;
+}
+
+}  // namespace
+
+std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
+                    bool with_transposes) {
+  std::string err = check_pattern(nb, rowptr, colind);
+  if (!err.empty()) return err;
+  an = Analysis();
+  an.nb = nb;
+  an.nnzb = rowptr[nb];
+  an.rowptr.assign(rowptr, rowptr + nb + 1);
+  an.colind.assign(colind, colind + an.nnzb);
+  an.color.resize(nb);
+  an.ncolors = color_greedy(nb, rowptr, colind, an.color.data());
+  const int C = an.ncolors;
+
+  // color-ordered permutation, natural order inside a color (counting sort)
+  an.color_ptr.assign(C + 1, 0);
+  for (int i = 0; i < nb; ++i) an.color_ptr[an.color[i] + 1]++;
+  for (int c = 0; c < C; ++c) an.color_ptr[c + 1] += an.color_ptr[c];
+  an.perm.resize(nb);
+  an.iperm.resize(nb);
+  {
+    std::vector<int> fill(an.color_ptr.begin(), an.color_ptr.end() - 1);
+    for (int i = 0; i < nb; ++i) an.perm[fill[an.color[i]]++] = i;
+  }
+  for (int i = 0; i < nb; ++i) an.iperm[an.perm[i]] = i;
+
+  // permuted pattern with sorted columns
+  an.prowptr.assign(static_cast<size_t>(nb) + 1, 0);
+  for (int i = 0; i < nb; ++i)
+    an.prowptr[i + 1] = an.prowptr[i] + (rowptr[an.perm[i] + 1] - rowptr[an.perm[i]]);
+  an.pcolind.resize(an.nnzb);
+  an.psrc.resize(an.nnzb);
+  an.pdiag.resize(nb);
+  std::vector<std::pair<int, int>> tmp;
+  for (int i = 0; i < nb; ++i) {
+    const int o = an.perm[i];
+    tmp.clear();
+    for (int k = rowptr[o]; k < rowptr[o + 1]; ++k) tmp.emplace_back(an.iperm[colind[k]], k);
+    std::sort(tmp.begin(), tmp.end());
+    for (size_t t = 0; t < tmp.size(); ++t) {
+      const int p = an.prowptr[i] + static_cast<int>(t);
+      an.pcolind[p] = tmp[t].first;
+      an.psrc[p] = tmp[t].second;
+      if (tmp[t].first == i) an.pdiag[i] = p;
+    }
+  }
+
+  // L / U / A row selections (src = permuted block index)
+  Csr a, l, u;
+  a.rowptr.assign(static_cast<size_t>(nb) + 1, 0);
+  l.rowptr = a.rowptr;
+  u.rowptr = a.rowptr;
+  for (int i = 0; i < nb; ++i) {
+    for (int k = an.prowptr[i]; k < an.prowptr[i + 1]; ++k) {
+      const int j = an.pcolind[k];
+      a.col.push_back(j); a.src.push_back(k);
+      if (j < i) { l.col.push_back(j); l.src.push_back(k); }
+      if (j > i) { u.col.push_back(j); u.src.push_back(k); }
+    }
+    a.rowptr[i + 1] = static_cast<int>(a.col.size());
+    l.rowptr[i + 1] = static_cast<int>(l.col.size());
+    u.rowptr[i + 1] = static_cast<int>(u.col.size());
+  }
+  an.nnzb_l = static_cast<int>(l.col.size());
+  an.nnzb_u = static_cast<int>(u.col.size());
+
+  // slices: 32 consecutive rows of one color
+  an.slice_color_ptr.assign(C + 1, 0);
+  for (int c = 0; c < C; ++c) {
+    const int rows = an.color_ptr[c + 1] - an.color_ptr[c];
+    const int ns = (rows + kSliceRows - 1) / kSliceRows;
+    an.slice_color_ptr[c + 1] = an.slice_color_ptr[c] + ns;
+    for (int s = 0; s < ns; ++s) {
+      an.slice_row0.push_back(an.color_ptr[c] + s * kSliceRows);
+      an.slice_len.push_back(std::min(kSliceRows, rows - s * kSliceRows));
+    }
+  }
+  an.S = an.slice_color_ptr[C];
+
+  slice_matrix(an, a, false, an.A);
+  slice_matrix(an, l, false, an.L);
+  slice_matrix(an, u, false, an.U);
+  if (with_transposes) {
+    slice_matrix(an, transpose_csr(nb, a), true, an.At);
+    // rows of U^T hold U_ij^T (i < j): lower part; rows of L^T: upper part
+    slice_matrix(an, transpose_csr(nb, u), true, an.Ut);
+    slice_matrix(an, transpose_csr(nb, l), true, an.Lt);
+  }
+  return "";
+}
+
+void permute_values(const Analysis &an, const double *vals, double *pvals) {
+  for (int k = 0; k < an.nnzb; ++k)
+    std::memcpy(pvals + static_cast<size_t>(k) * 9,
+                vals + static_cast<size_t>(an.psrc[k]) * 9, 9 * sizeof(double));
+}
+
+namespace {
+
+// 3x3 inverse via cofactors; false when singular or not finite.
+bool inv3(const double *a, double *o) {
+  const double c00 = a[4] * a[8] - a[5] * a[7];
+  const double c01 = a[5] * a[6] - a[3] * a[8];
+  const double c02 = a[3] * a[7] - a[4] * a[6];
+  const double det = a[0] * c00 + a[1] * c01 + a[2] * c02;
+  if (det == 0.0 || !std::isfinite(det)) return false;
+  const double id = 1.0 / det;
+  o[0] = c00 * id;
+  o[1] = (a[2] * a[7] - a[1] * a[8]) * id;
+  o[2] = (a[1] * a[5] - a[2] * a[4]) * id;
+  o[3] = c01 * id;
+  o[4] = (a[0] * a[8] - a[2] * a[6]) * id;
+  o[5] = (a[2] * a[3] - a[0] * a[5]) * id;
+  o[6] = c02 * id;
+  o[7] = (a[1] * a[6] - a[0] * a[7]) * id;
+  o[8] = (a[0] * a[4] - a[1] * a[3]) * id;
+  return true;
+}
+
+inline void mul3(const double *a, const double *b, double *o) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      o[r * 3 + c] = a[r * 3] * b[c] + a[r * 3 + 1] * b[3 + c] + a[r * 3 + 2] * b[6 + c];
+}
+
+}  // namespace
+
+int bilu0(const Analysis &an, double *v, double *dinv) {
+  // IKJ block ILU(0): for row i and each k < i in row i, L_ik = A_ik U_kk^-1,
+  // then A_ij -= L_ik U_kj for every j > k present in both rows i and k.
+  const int nb = an.nb;
+  std::vector<int> pos(nb, -1);
+  for (int i = 0; i < nb; ++i) {
+    for (int k = an.prowptr[i]; k < an.prowptr[i + 1]; ++k) pos[an.pcolind[k]] = k;
+    for (int kk = an.prowptr[i]; kk < an.pdiag[i]; ++kk) {
+      const int k = an.pcolind[kk];
+      double l[9];
+      mul3(v + static_cast<size_t>(kk) * 9, dinv + static_cast<size_t>(k) * 9, l);
+      std::memcpy(v + static_cast<size_t>(kk) * 9, l, sizeof l);
+      for (int jj = an.pdiag[k] + 1; jj < an.prowptr[k + 1]; ++jj) {
+        const int p = pos[an.pcolind[jj]];
+        if (p < 0) continue;
+        double t[9];
+        mul3(l, v + static_cast<size_t>(jj) * 9, t);
+        double *dst = v + static_cast<size_t>(p) * 9;
+        for (int e = 0; e < 9; ++e) dst[e] -= t[e];
+      }
+    }
+    if (!inv3(v + static_cast<size_t>(an.pdiag[i]) * 9, dinv + static_cast<size_t>(i) * 9))
+      return i;
+    for (int k = an.prowptr[i]; k < an.prowptr[i + 1]; ++k) pos[an.pcolind[k]] = -1;
+  }
+  return -1;
+}
+
+template <typename V>
+void fill_sliced(const SlicedMatrix &m, const double *src, V *out) {
+  const size_t slots = static_cast<size_t>(m.slots());
+  for (size_t slot = 0; slot < slots; ++slot)
+    for (int l = 0; l < kSliceRows; ++l) {
+      const int s = m.vsrc[slot * kSliceRows + l];
+      for (int e = 0; e < 9; ++e) {
+        double x = 0.0;
+        if (s >= 0) {
+          const int ee = m.transpose_blocks ? (e % 3) * 3 + e / 3 : e;
+          x = src[static_cast<size_t>(s) * 9 + ee];
+        }
+        out[(slot * 9 + e) * kSliceRows + l] = static_cast<V>(x);
+      }
+    }
+}
+
+template <typename V>
+void fill_sliced_diag(const Analysis &an, const double *d, bool transpose, V *out) {
+  for (int s = 0; s < an.S; ++s)
+    for (int l = 0; l < kSliceRows; ++l) {
+      const int r = an.slice_row0[s] + l;
+      for (int e = 0; e < 9; ++e) {
+        double x = 0.0;
+        if (l < an.slice_len[s]) {
+          const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
+          x = d[static_cast<size_t>(r) * 9 + ee];
+        }
+        out[(static_cast<size_t>(s) * 9 + e) * kSliceRows + l] = static_cast<V>(x);
+      }
+    }
+}
+
+template void fill_sliced<double>(const SlicedMatrix &, const double *, double *);
+template void fill_sliced<float>(const SlicedMatrix &, const double *, float *);
+template void fill_sliced_diag<double>(const Analysis &, const double *, bool, double *);
+template void fill_sliced_diag<float>(const Analysis &, const double *, bool, float *);
+
+}  // namespace gbilu

@@ -1,0 +1,81 @@
+// Host-side analysis for the GB300 ILU0-BiCGSTAB path: greedy block coloring,
+// color-ordered permutation, block ILU0 factorization and the sliced device
+// layout. Plain C++ (no CUDA): the same code runs in host-only handles.
+//
+// In the reference these steps happen in the Flow backend before the FPGA
+// host library is called; the library only receives their output through
+// vectorPointers (linearalgebra/ilu0bicgstab/xilinx/src/sda_app/common/
+// fpga_functions_bicgstab.cpp:506-629).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace gbilu {
+
+constexpr int kSliceRows = 32;  // block rows per slice = one warp
+
+// One matrix (A, L, U or a transpose) in the sliced layout shared by all
+// matrices of a handle. Slice s covers block rows slice_row0[s] ..
+// slice_row0[s] + slice_len[s] - 1 of one color; row lane l of slice s keeps
+// its k-th block in slot off[s] + k: column col[slot*32 + l] (-1 = padding,
+// always after the row's last block) and value entry e at
+// val[(slot*9 + e)*32 + l]. Blocks of a row are in ascending column order.
+struct SlicedMatrix {
+  std::vector<int> off;   // [S+1]
+  std::vector<int> col;   // [slots*32]
+  std::vector<int> vsrc;  // [slots*32] source block in the value array, -1 pad
+  bool transpose_blocks = false;  // fill with the transposed 3x3 block
+  long long slots() const { return off.empty() ? 0 : off.back(); }
+};
+
+struct Analysis {
+  int nb = 0, nnzb = 0, ncolors = 0;
+  std::vector<int> rowptr, colind;        // input pattern
+  std::vector<int> color;                 // [nb] color of input row
+  std::vector<int> perm, iperm;           // perm[new] = old
+  std::vector<int> color_ptr;             // [C+1] new-index range per color
+  std::vector<int> prowptr, pcolind;      // permuted pattern, sorted columns
+  std::vector<int> psrc;                  // permuted block -> input block
+  std::vector<int> pdiag;                 // position of the diagonal block
+  int nnzb_l = 0, nnzb_u = 0;
+  // slices
+  int S = 0;
+  std::vector<int> slice_color_ptr;       // [C+1]
+  std::vector<int> slice_row0, slice_len; // [S]
+  SlicedMatrix A, L, U;                   // forward operators
+  SlicedMatrix At, Ut, Lt;                // transposed operators (adjoint)
+};
+
+// Greedy first-fit coloring in natural row order; returns the color count.
+int color_greedy(int nb, const int *rowptr, const int *colind, int *color);
+
+// Validates the pattern (sorted unique columns, diagonal present, indices in
+// range); returns an empty string when it is fine.
+std::string check_pattern(int nb, const int *rowptr, const int *colind);
+
+// Builds everything above from an input pattern. Returns "" or an error.
+std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
+                    bool with_transposes);
+
+// Block ILU(0) (IKJ) of the permuted matrix. pvals (nnzb*9, permuted order)
+// is overwritten with L (col < row) and U (col >= row); dinv[nb*9] gets the
+// inverses of U's diagonal blocks. Returns -1 or the first singular row.
+int bilu0(const Analysis &an, double *pvals, double *dinv);
+
+// Gathers input-order values into the permuted order.
+void permute_values(const Analysis &an, const double *vals, double *pvals);
+
+// Fills a sliced value array (slots*9*32 entries of type V) from a value
+// source array (9 doubles per block); padding entries become 0.
+template <typename V>
+void fill_sliced(const SlicedMatrix &m, const double *src, V *out);
+
+// Sliced copy of per-row 3x3 blocks (nb*9 doubles in permuted row order),
+// optionally transposed, laid out [(slice*9 + e)*32 + lane].
+template <typename V>
+void fill_sliced_diag(const Analysis &an, const double *dinv, bool transpose,
+                      V *out);
+
+}  // namespace gbilu

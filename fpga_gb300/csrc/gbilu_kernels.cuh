@@ -1,0 +1,537 @@
+// Device kernels of the GB300 ILU0-BiCGSTAB path (sm_103a).
+//
+// Every kernel is memory-streaming work on the sliced layout described in
+// gbilu_host.hpp: one thread owns one block row (3 unknowns), a warp owns a
+// 32-row slice, and each of the 9 block entries of a slot is one coalesced
+// 32-lane load. Dot products and norms are fused into the kernel that
+// produces the vector; per-CTA partials are combined by the last CTA to
+// finish ("last block" pattern, no spinning), in a fixed order, so every
+// result is bit-for-bit reproducible from run to run.
+//
+// Solver scalars never leave the device: they live in a Ctl block that the
+// fused kernels update; every kernel of an iteration returns at once when
+// Ctl::done is set, which lets a fixed CUDA graph run the loop.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace gbilu {
+
+constexpr int kThreads = 256;                 // threads per CTA
+constexpr int kWarps = kThreads / 32;
+constexpr double kAlreadySolved = 1e-30;      // constants.vhd:59
+
+enum Status {
+  ST_OK = 0, ST_MAXIT = 1, ST_ALREADY = 2, ST_BREAKDOWN = 3, ST_NONFINITE = 4,
+  ST_TIMEOUT = 5
+};
+
+// Device-resident solver state, one per solve in flight.
+struct Ctl {
+  double rho, alpha, omega, beta;
+  double bound, norm0, norm, tol;
+  double norms[4];
+  double dots[4];                 // last reduced values (diagnostics)
+  int absolute, maxit;
+  int last_norm_idx;
+  int half;                       // the reference's half-iteration counter
+  int k;                          // current full iteration
+  int done, status, stop_half;    // stop_half: stopped after a first half
+  unsigned long long t_start, timeout_ns;
+  unsigned int counter[8];        // arrival counters of the last-block pattern
+};
+
+// --------------------------------------------------------------------------
+// small helpers
+// --------------------------------------------------------------------------
+
+template <typename T> __device__ __forceinline__ T ldg_stream(const T *p) { return __ldcs(p); }
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool finite(double v) { return isfinite(v); }
+
+// Exact product and error-free sum on the FP32 pipe: a double-float
+// accumulator (hi + lo) that keeps ~44 bits, so FP32 vectors get dot products
+// of FP64 quality without touching GB300's slow FP64 units per element.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ void df_add_prod(DF &acc, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);             // a*b = p + e exactly
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += err + e;
+}
+__device__ __forceinline__ double df_value(const DF &a) { return (double)a.hi + (double)a.lo; }
+
+// Deterministic block reduction of NV doubles; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double red[NV][kWarps];
+#pragma unroll
+  for (int j = 0; j < NV; ++j)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) red[j][w] = v[j];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double x = l < kWarps ? red[j][l] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      v[j] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// Writes this CTA's partials and returns true in every thread of the CTA
+// that arrives last; that CTA then holds the fixed-order grid totals in tot.
+template <int NV>
+__device__ __forceinline__ bool grid_sum(double (&v)[NV], double *partials,
+                                         unsigned int *counter, double (&tot)[NV]) {
+  __shared__ bool last;
+  __shared__ double res[NV];
+  block_sum<NV>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) partials[(size_t)j * gridDim.x + blockIdx.x] = v[j];
+    __threadfence();
+    const unsigned int prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    acc[j] = 0.0;
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+      acc[j] += __ldcg(partials + (size_t)j * gridDim.x + b);
+  }
+  block_sum<NV>(acc);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) res[j] = acc[j];
+    *counter = 0u;                               // ready for the next kernel
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) tot[j] = res[j];
+  return true;
+}
+
+// the m-th norm after the initial one goes to ring slot (half % 3) + 1
+// (solver.vhd:913-918, bicgstab_utils.cpp:256)
+__device__ __forceinline__ void push_norm(Ctl *c, double nrm) {
+  const int idx = (c->half % 3) + 1;
+  c->norms[idx] = nrm;
+  c->last_norm_idx = idx;
+  c->norm = nrm;
+}
+
+__device__ __forceinline__ void stop(Ctl *c, int status, int stop_half) {
+  c->status = status;
+  c->stop_half = stop_half;
+  c->done = 1;
+}
+
+// --------------------------------------------------------------------------
+// control
+// --------------------------------------------------------------------------
+
+__global__ void k_ctl_init(Ctl *c, double tol, int absolute, int maxit,
+                           unsigned long long timeout_ns) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    c->rho = c->alpha = c->omega = c->beta = 0.0;
+    c->bound = c->norm0 = c->norm = 0.0;
+    c->tol = tol;
+    for (int i = 0; i < 4; ++i) { c->norms[i] = 0.0; c->dots[i] = 0.0; }
+    c->absolute = absolute;
+    c->maxit = maxit;
+    c->last_norm_idx = 0;
+    c->half = -1;
+    c->k = 0;
+    c->done = 0;
+    c->status = ST_MAXIT;
+    c->stop_half = 0;
+    c->t_start = globaltimer();
+    c->timeout_ns = timeout_ns;
+    for (int i = 0; i < 8; ++i) c->counter[i] = 0u;
+  }
+}
+
+// Steps 0/1 of the PROGRAM (solver_pkg.vhd:122-123, solver.vhd:887-911):
+// r = b - A x0, rho = ||r||^2, the "already solved" test and the absolute
+// stopping bound. MODE 0: r = b - A x (vals/x given); MODE 1: r = b (x0 = 0,
+// used by the inner solves of iterative refinement).
+template <typename T>
+__device__ __forceinline__ void finish_init(Ctl *c, double rr) {
+  const double n0 = sqrt(rr);
+  c->norm0 = n0;
+  c->norm = n0;
+  c->norms[0] = n0;
+  c->last_norm_idx = 0;
+  c->rho = rr;
+  double bound = c->absolute ? c->tol : kAlreadySolved;
+  if (!finite(n0)) { stop(c, ST_NONFINITE, 0); return; }
+  if (!(n0 > bound)) { stop(c, ST_ALREADY, 0); return; }
+  if (!c->absolute) bound = c->tol * n0;
+  c->bound = bound;
+  c->half = 0;
+  c->k = 0;
+}
+
+// --------------------------------------------------------------------------
+// sliced SpMV with fused reductions
+// --------------------------------------------------------------------------
+
+enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3 };
+
+// y = A x over all slices. RESID: y = b - A x, ||y||^2 -> init. ALPHA:
+// (y, w) -> alpha = rho/(y,w) (step 5). OMEGA: (y, w), (y, y) ->
+// omega = (y,w)/(y,y) (step 10). V: matrix value type, T: vector type.
+template <typename V, typename T, int MODE>
+__global__ void __launch_bounds__(kThreads)
+k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
+       const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
+       T *__restrict__ y, const T *__restrict__ w, double *partials) {
+  if (MODE != SPMV_PLAIN && MODE != SPMV_RESID && ctl->done) return;
+  const int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  double d1 = 0.0, d2 = 0.0;
+  DF f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
+  if (s < S) {
+    const int2 sr = srows[s];
+    if (lane < sr.y) {
+      const int row = sr.x + lane;
+      const int o = off[s], wdt = off[s + 1] - o;
+      T a0 = 0, a1 = 0, a2 = 0;
+      for (int k = 0; k < wdt; ++k) {
+        const size_t slot = (size_t)(o + k);
+        const int c = ldg_stream(col + slot * 32 + lane);
+        if (c < 0) break;
+        const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
+        const V *v = val + slot * 9 * 32 + lane;
+        a0 = fma((T)ldg_stream(v + 0 * 32), x0, a0);
+        a0 = fma((T)ldg_stream(v + 1 * 32), x1, a0);
+        a0 = fma((T)ldg_stream(v + 2 * 32), x2, a0);
+        a1 = fma((T)ldg_stream(v + 3 * 32), x0, a1);
+        a1 = fma((T)ldg_stream(v + 4 * 32), x1, a1);
+        a1 = fma((T)ldg_stream(v + 5 * 32), x2, a1);
+        a2 = fma((T)ldg_stream(v + 6 * 32), x0, a2);
+        a2 = fma((T)ldg_stream(v + 7 * 32), x1, a2);
+        a2 = fma((T)ldg_stream(v + 8 * 32), x2, a2);
+      }
+      if (MODE == SPMV_RESID) {
+        a0 = w[3 * row] - a0; a1 = w[3 * row + 1] - a1; a2 = w[3 * row + 2] - a2;
+      }
+      y[3 * row] = a0; y[3 * row + 1] = a1; y[3 * row + 2] = a2;
+      if (MODE == SPMV_RESID) {
+        if (sizeof(T) == 8) d1 = (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
+        else { df_add_prod(f1, (float)a0, (float)a0); df_add_prod(f1, (float)a1, (float)a1); df_add_prod(f1, (float)a2, (float)a2); }
+      } else if (MODE == SPMV_ALPHA || MODE == SPMV_OMEGA) {
+        const T w0 = w[3 * row], w1 = w[3 * row + 1], w2 = w[3 * row + 2];
+        if (sizeof(T) == 8) {
+          d1 = (double)a0 * w0 + (double)a1 * w1 + (double)a2 * w2;
+          if (MODE == SPMV_OMEGA) d2 = (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
+        } else {
+          df_add_prod(f1, (float)a0, (float)w0); df_add_prod(f1, (float)a1, (float)w1); df_add_prod(f1, (float)a2, (float)w2);
+          if (MODE == SPMV_OMEGA) { df_add_prod(f2, (float)a0, (float)a0); df_add_prod(f2, (float)a1, (float)a1); df_add_prod(f2, (float)a2, (float)a2); }
+        }
+      }
+    }
+  }
+  if (MODE == SPMV_PLAIN) return;
+  if (sizeof(T) == 4) { d1 = df_value(f1); d2 = df_value(f2); }
+  if (MODE == SPMV_RESID) {
+    double v[1] = {d1}, tot[1];
+    if (grid_sum<1>(v, partials, &ctl->counter[0], tot) && threadIdx.x == 0)
+      finish_init<T>(ctl, tot[0]);
+  } else if (MODE == SPMV_ALPHA) {
+    double v[1] = {d1}, tot[1];
+    if (grid_sum<1>(v, partials, &ctl->counter[1], tot) && threadIdx.x == 0) {
+      const double a = ctl->rho / tot[0];
+      ctl->dots[0] = tot[0];
+      ctl->alpha = a;
+      if (tot[0] == 0.0 || !finite(a)) stop(ctl, ST_BREAKDOWN, 0);
+    }
+  } else {
+    double v[2] = {d1, d2}, tot[2];
+    if (grid_sum<2>(v, partials, &ctl->counter[2], tot) && threadIdx.x == 0) {
+      const double om = tot[0] / tot[1];
+      ctl->dots[1] = tot[0];
+      ctl->dots[2] = tot[1];
+      ctl->omega = om;
+      // half 1 already advanced x by alpha p^: keep it on a stop here
+      if (tot[1] == 0.0 || !finite(om)) stop(ctl, ST_BREAKDOWN, 1);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// one color of a triangular sweep
+// --------------------------------------------------------------------------
+
+// dst_i = [D_i] (src_i - sum_j B_ij nbr_j) for the rows of one color.
+// L sweep: B = L, src = p, nbr = dst = p^ (colors ascending; ilu0.vhd:413-416);
+// U sweep: B = U, D = Dinv, src = nbr = dst = p^ (colors descending;
+// ilu0.vhd:293-323,407-411). The same kernel runs the transposed sweeps of
+// the adjoint with B = U^T (D = Dinv^T) and B = L^T.
+template <typename V, typename T, bool HAS_D>
+__global__ void __launch_bounds__(kThreads)
+k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__ off,
+        const int *__restrict__ col, const V *__restrict__ val, const V *__restrict__ dmat,
+        const T *src, const T *nbr, T *dst) {
+  if (ctl->done) return;
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= nrows) return;
+  const int row = row0 + t;
+  const int s = slice0 + (t >> 5), lane = t & 31;
+  const int o = off[s], wdt = off[s + 1] - o;
+  T a0 = src[3 * row], a1 = src[3 * row + 1], a2 = src[3 * row + 2];
+  for (int k = 0; k < wdt; ++k) {
+    const size_t slot = (size_t)(o + k);
+    const int c = ldg_stream(col + slot * 32 + lane);
+    if (c < 0) break;
+    const T y0 = nbr[3 * c], y1 = nbr[3 * c + 1], y2 = nbr[3 * c + 2];
+    const V *v = val + slot * 9 * 32 + lane;
+    a0 = fma(-(T)ldg_stream(v + 0 * 32), y0, a0);
+    a0 = fma(-(T)ldg_stream(v + 1 * 32), y1, a0);
+    a0 = fma(-(T)ldg_stream(v + 2 * 32), y2, a0);
+    a1 = fma(-(T)ldg_stream(v + 3 * 32), y0, a1);
+    a1 = fma(-(T)ldg_stream(v + 4 * 32), y1, a1);
+    a1 = fma(-(T)ldg_stream(v + 5 * 32), y2, a1);
+    a2 = fma(-(T)ldg_stream(v + 6 * 32), y0, a2);
+    a2 = fma(-(T)ldg_stream(v + 7 * 32), y1, a2);
+    a2 = fma(-(T)ldg_stream(v + 8 * 32), y2, a2);
+  }
+  if (HAS_D) {
+    const V *d = dmat + (size_t)s * 9 * 32 + lane;
+    const T z0 = (T)d[0 * 32] * a0 + (T)d[1 * 32] * a1 + (T)d[2 * 32] * a2;
+    const T z1 = (T)d[3 * 32] * a0 + (T)d[4 * 32] * a1 + (T)d[5 * 32] * a2;
+    const T z2 = (T)d[6 * 32] * a0 + (T)d[7 * 32] * a1 + (T)d[8 * 32] * a2;
+    a0 = z0; a1 = z1; a2 = z2;
+  }
+  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+}
+
+// --------------------------------------------------------------------------
+// fused vector kernels (grid-stride over the n unknowns)
+// --------------------------------------------------------------------------
+
+// After step 1: rt = p = r; p^ = r on the first color's unknowns (the L sweep
+// of color 0 is the identity, so its output is written here instead).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_init_vectors(const Ctl *ctl, int n, int n0, const T *__restrict__ r, T *__restrict__ rt,
+               T *__restrict__ p, T *__restrict__ ph) {
+  if (ctl->done) return;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const T v = r[i];
+    rt[i] = v;
+    p[i] = v;
+    if (i < n0) ph[i] = v;
+  }
+}
+
+// Inner solves of iterative refinement start from d = 0: r = rt = p = rhs,
+// rho = ||rhs||^2 (step 1 without the SpMV of step 0).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_init_rhs(Ctl *ctl, int n, int n0, const T *__restrict__ rhs, T *__restrict__ r,
+           T *__restrict__ rt, T *__restrict__ p, T *__restrict__ ph, T *__restrict__ x,
+           double *partials) {
+  double d = 0.0;
+  DF f = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const T v = rhs[i];
+    r[i] = v; rt[i] = v; p[i] = v; x[i] = 0;
+    if (i < n0) ph[i] = v;
+    if (sizeof(T) == 8) d += (double)v * v; else df_add_prod(f, (float)v, (float)v);
+  }
+  if (sizeof(T) == 4) d = df_value(f);
+  double v[1] = {d}, tot[1];
+  if (grid_sum<1>(v, partials, &ctl->counter[0], tot) && threadIdx.x == 0)
+    finish_init<T>(ctl, tot[0]);
+}
+
+// Steps 6-8 without the x update (deferred to the second half): s = r - alpha v,
+// ||s|| and the stop tests (solver.vhd:867-936, is_final_iter solver.vhd:557);
+// s^ = s on the first color's unknowns.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_update_s(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
+           T *__restrict__ s, T *__restrict__ sh, double *partials) {
+  if (ctl->done) return;
+  const T alpha = (T)ctl->alpha;
+  double d = 0.0;
+  DF f = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const T si = fma(-alpha, v[i], r[i]);
+    s[i] = si;
+    if (i < n0) sh[i] = si;
+    if (sizeof(T) == 8) d += (double)si * si; else df_add_prod(f, (float)si, (float)si);
+  }
+  if (sizeof(T) == 4) d = df_value(f);
+  double vv[1] = {d}, tot[1];
+  if (grid_sum<1>(vv, partials, &ctl->counter[3], tot) && threadIdx.x == 0) {
+    const double ns = sqrt(tot[0]);
+    push_norm(ctl, ns);
+    if (!finite(ns)) stop(ctl, ST_NONFINITE, 1);
+    else if (!(ns > ctl->bound)) stop(ctl, ST_OK, 1);
+    else if (ctl->k == ctl->maxit) stop(ctl, ST_MAXIT, 1);
+    else ctl->half = 2 * ctl->k + 1;
+  }
+}
+
+// Steps 11-14: x += alpha p^ + omega s^ (both halves' updates in one pass),
+// r = s - omega t, ||r||, rho' = (r, rt), beta = (rho'/rho)(alpha/omega).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
+           const T *__restrict__ sh, const T *__restrict__ s, const T *__restrict__ t,
+           const T *__restrict__ rt, T *__restrict__ r, double *partials) {
+  if (ctl->done) return;
+  const T alpha = (T)ctl->alpha, omega = (T)ctl->omega;
+  double d1 = 0.0, d2 = 0.0;
+  DF f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    x[i] = fma(omega, sh[i], fma(alpha, ph[i], x[i]));
+    const T ri = fma(-omega, t[i], s[i]);
+    r[i] = ri;
+    const T rti = rt[i];
+    if (sizeof(T) == 8) { d1 += (double)ri * ri; d2 += (double)ri * rti; }
+    else { df_add_prod(f1, (float)ri, (float)ri); df_add_prod(f2, (float)ri, (float)rti); }
+  }
+  if (sizeof(T) == 4) { d1 = df_value(f1); d2 = df_value(f2); }
+  double vv[2] = {d1, d2}, tot[2];
+  if (grid_sum<2>(vv, partials, &ctl->counter[4], tot) && threadIdx.x == 0) {
+    const double nr = sqrt(tot[0]);
+    push_norm(ctl, nr);
+    ctl->dots[3] = tot[1];
+    if (!finite(nr)) { stop(ctl, ST_NONFINITE, 0); return; }
+    if (!(nr > ctl->bound)) { stop(ctl, ST_OK, 0); return; }
+    const double rho_new = tot[1];
+    const double beta = (rho_new / ctl->rho) * (ctl->alpha / ctl->omega);
+    ctl->rho = rho_new;
+    ctl->beta = beta;
+    if (ctl->omega == 0.0 || !finite(beta)) { stop(ctl, ST_BREAKDOWN, 0); return; }
+    if (ctl->timeout_ns && globaltimer() - ctl->t_start > ctl->timeout_ns) {
+      stop(ctl, ST_TIMEOUT, 0);
+      return;
+    }
+    ctl->k += 1;
+    ctl->half = 2 * ctl->k;
+  }
+}
+
+// Steps 15-17 (update_p, vector_ops.vhd:429-434): p = r + beta (p - omega v);
+// p^ = p on the first color's unknowns. Also drives the graph's while loop.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_update_p(const Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
+           T *__restrict__ p, T *__restrict__ ph, unsigned long long cond) {
+  if (cond && blockIdx.x == 0 && threadIdx.x == 0)
+    cudaGraphSetConditional((cudaGraphConditionalHandle)cond, ctl->done ? 0u : 1u);
+  if (ctl->done) return;
+  const T beta = (T)ctl->beta, omega = (T)ctl->omega;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const T pi = fma(beta, fma(-omega, v[i], p[i]), r[i]);
+    p[i] = pi;
+    if (i < n0) ph[i] = pi;
+  }
+}
+
+// After the loop: a stop after a first half still owes x += alpha p^.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_finish_x(const Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph) {
+  if (!ctl->stop_half) return;
+  const T alpha = (T)ctl->alpha;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    x[i] = fma(alpha, ph[i], x[i]);
+}
+
+// --------------------------------------------------------------------------
+// permutation, precision conversion, refinement and gradient kernels
+// --------------------------------------------------------------------------
+
+// out[3i+r] = in[3 perm[i] + r]  (original -> permuted numbering)
+template <typename TI, typename TO>
+__global__ void k_gather(int nb, const int *__restrict__ perm, const TI *__restrict__ in,
+                         TO *__restrict__ out, double scale) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < 3 * nb; i += gridDim.x * kThreads) {
+    const int b = i / 3, r = i - 3 * b;
+    out[i] = (TO)((double)in[3 * perm[b] + r] * scale);
+  }
+}
+
+// out[3 perm[i] + r] = in[3i+r]  (permuted -> original numbering)
+template <typename T>
+__global__ void k_scatter(int nb, const int *__restrict__ perm, const T *__restrict__ in,
+                          T *__restrict__ out) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < 3 * nb; i += gridDim.x * kThreads) {
+    const int b = i / 3, r = i - 3 * b;
+    out[3 * perm[b] + r] = in[i];
+  }
+}
+
+// out = (float)(scale * in): the FP32 right-hand side of a refinement step
+__global__ void k_scale_convert(int n, double scale, const double *__restrict__ in,
+                                float *__restrict__ out) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    out[i] = (float)(scale * in[i]);
+}
+
+// x += scale * d (FP64 x, FP32 correction of one refinement step)
+__global__ void k_axpy_f2d(int n, double scale, const float *__restrict__ d,
+                           double *__restrict__ x) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    x[i] = fma(scale, (double)d[i], x[i]);
+}
+
+// ||v||^2 into ctl->dots[0] (refinement residual norm), FP64
+__global__ void __launch_bounds__(kThreads)
+k_norm2(Ctl *ctl, int n, const double *__restrict__ v, double *partials) {
+  double d = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    d += v[i] * v[i];
+  double vv[1] = {d}, tot[1];
+  if (grid_sum<1>(vv, partials, &ctl->counter[5], tot) && threadIdx.x == 0)
+    ctl->dots[0] = tot[0];
+}
+
+// dA[src[k]] = -lambda_i x_j^T for the blocks k of permuted row i
+// (the pattern gradient of L(x(A)), x = A^-1 b).
+__global__ void k_grad_a(int nb, const int *__restrict__ prowptr, const int *__restrict__ pcol,
+                         const int *__restrict__ psrc, const double *__restrict__ lam,
+                         const double *__restrict__ x, double *__restrict__ dA) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < nb; i += gridDim.x * kThreads) {
+    const double l0 = lam[3 * i], l1 = lam[3 * i + 1], l2 = lam[3 * i + 2];
+    for (int k = prowptr[i]; k < prowptr[i + 1]; ++k) {
+      const int j = pcol[k];
+      const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+      double *o = dA + (size_t)psrc[k] * 9;
+      o[0] = -l0 * x0; o[1] = -l0 * x1; o[2] = -l0 * x2;
+      o[3] = -l1 * x0; o[4] = -l1 * x1; o[5] = -l1 * x2;
+      o[6] = -l2 * x0; o[7] = -l2 * x1; o[8] = -l2 * x2;
+    }
+  }
+}
+
+}  // namespace gbilu

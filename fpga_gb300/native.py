@@ -1,0 +1,241 @@
+"""ctypes binding of libgbilu.so (the C ABI declared in include/gbilu.h).
+
+There is no fallback: if the library is missing or fails to load, every call
+raises. Build it with ``fpga_gb300.build.build_library()`` (or
+``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from .build import LIB, ROOT
+
+HEADER = os.path.join(ROOT, "include", "gbilu.h")
+
+OK, MAXIT, ALREADY_CONVERGED, BREAKDOWN, NONFINITE, TIMEOUT = 0, 1, 2, 3, 4, 5
+BAD_INPUT, SINGULAR, CUDA_ERROR, NOT_READY, NO_DEVICE = 6, 7, 8, 9, 10
+FP64, MIXED = 0, 1
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("absolute_tol", C.c_int), ("device", C.c_int),
+                ("use_graph", C.c_int), ("timeout_ms", C.c_double),
+                ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
+                ("max_outer", C.c_int), ("verbose", C.c_int)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("half_iters", C.c_int), ("iterations", C.c_double),
+                ("norm0", C.c_double), ("norm", C.c_double), ("relres", C.c_double),
+                ("norms", C.c_double * 4), ("last_norm_idx", C.c_int),
+                ("outer_iters", C.c_int), ("inner_half_iters", C.c_int),
+                ("true_relres", C.c_double), ("device_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["norms"] = list(self.norms)
+        return d
+
+
+class Stats(C.Structure):
+    _fields_ = [("nb", C.c_int), ("nnzb", C.c_int), ("ncolors", C.c_int),
+                ("nnzb_lower", C.c_int), ("nnzb_upper", C.c_int), ("slices", C.c_int),
+                ("slots_a", C.c_longlong), ("slots_l", C.c_longlong),
+                ("slots_u", C.c_longlong), ("device_bytes", C.c_longlong),
+                ("launches_per_iter", C.c_int), ("last_launches", C.c_longlong),
+                ("factor_ms", C.c_double), ("analyze_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class GbIluError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gbilu error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+I32P = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+F64P = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+VP = C.c_void_p
+
+
+def declared_symbols():
+    """Function names declared in include/gbilu.h."""
+    with open(HEADER) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^(?:int|const char \*)\s*(gbilu_\w+)\s*\(", text, re.M)))
+
+
+def load():
+    """Loads libgbilu.so; raises if it is absent (there is no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise RuntimeError(f"{LIB} is missing: build it with fpga_gb300.build.build_library()")
+    L = C.CDLL(LIB)
+    L.gbilu_default_options.argtypes = [C.POINTER(Options)]
+    L.gbilu_create.argtypes = [C.POINTER(Options), C.POINTER(VP)]
+    L.gbilu_destroy.argtypes = [VP]
+    L.gbilu_analyze.argtypes = [VP, C.c_int, I32P, I32P]
+    L.gbilu_get_ordering.argtypes = [VP, C.POINTER(C.c_int), VP, VP, VP]
+    L.gbilu_factor.argtypes = [VP, F64P]
+    L.gbilu_get_factors.argtypes = [VP, VP, VP]
+    L.gbilu_solve.argtypes = [VP, VP, VP, C.c_double, C.c_int, C.POINTER(Result)]
+    L.gbilu_solve_device.argtypes = [VP, VP, VP, C.c_double, C.c_int, C.POINTER(Result)]
+    L.gbilu_apply_spmv.argtypes = [VP, F64P, F64P, C.c_int]
+    L.gbilu_apply_ilu.argtypes = [VP, F64P, F64P, C.c_int]
+    L.gbilu_adjoint.argtypes = [VP, F64P, F64P, F64P, VP, C.c_double, C.c_int,
+                                C.POINTER(Result)]
+    L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
+    L.gbilu_status_string.argtypes = [C.c_int]
+    L.gbilu_status_string.restype = C.c_char_p
+    L.gbilu_last_error.argtypes = [VP]
+    L.gbilu_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class GbIlu:
+    """One solver handle: analyze a pattern once, factor values, solve.
+
+    Mirrors the C ABI one to one; every failure raises GbIluError carrying
+    the library's status code and message.
+    """
+
+    def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
+                 timeout_ms=0.0, inner_tol=1e-4, inner_maxit=500, max_outer=30,
+                 verbose=0):
+        self.L = load()
+        o = Options()
+        self.L.gbilu_default_options(C.byref(o))
+        o.precision = MIXED if precision == "mixed" else FP64
+        o.device = device
+        o.use_graph = int(use_graph)
+        o.absolute_tol = int(absolute)
+        o.timeout_ms = timeout_ms
+        o.inner_tol = inner_tol
+        o.inner_maxit = inner_maxit
+        o.max_outer = max_outer
+        o.verbose = verbose
+        self.h = VP()
+        rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
+        if rc:
+            raise GbIluError(rc, "gbilu_create failed")
+        self.nb = 0
+        self.nnzb = 0
+
+    def _check(self, rc):
+        if rc:
+            raise GbIluError(rc, self.L.gbilu_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.L.gbilu_destroy(self.h)
+            self.h = VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # --- set-up
+    def analyze(self, rowptr, colind):
+        rowptr = np.ascontiguousarray(rowptr, dtype=np.int32)
+        colind = np.ascontiguousarray(colind, dtype=np.int32)
+        self.nb = rowptr.size - 1
+        self.nnzb = int(rowptr[-1]) if rowptr.size else 0
+        self._check(self.L.gbilu_analyze(self.h, self.nb, rowptr, colind))
+        return self
+
+    def factor(self, vals):
+        v = _f64(vals).reshape(-1)
+        if v.size != 9 * self.nnzb:
+            raise ValueError("vals must hold nnzb*9 doubles")
+        self._check(self.L.gbilu_factor(self.h, v))
+        return self
+
+    def ordering(self):
+        nc = C.c_int()
+        self._check(self.L.gbilu_get_ordering(self.h, C.byref(nc), None, None, None))
+        color = np.empty(self.nb, np.int32)
+        perm = np.empty(self.nb, np.int32)
+        cp = np.empty(nc.value + 1, np.int32)
+        self._check(self.L.gbilu_get_ordering(self.h, C.byref(nc), color.ctypes.data,
+                                              perm.ctypes.data, cp.ctypes.data))
+        return nc.value, color, perm, cp
+
+    def factors(self):
+        lu = np.empty(9 * self.nnzb)
+        dinv = np.empty(9 * self.nb)
+        self._check(self.L.gbilu_get_factors(self.h, lu.ctypes.data, dinv.ctypes.data))
+        return lu, dinv
+
+    # --- compute
+    def solve(self, b, x0=None, tol=1e-2, maxit=200):
+        b = _f64(b)
+        x = np.zeros(3 * self.nb) if x0 is None else _f64(x0).copy()
+        res = Result()
+        self._check(self.L.gbilu_solve(self.h, b.ctypes.data, x.ctypes.data, tol, maxit,
+                                       C.byref(res)))
+        return x, res
+
+    def solve_device(self, b_ptr, x_ptr, tol=1e-2, maxit=200):
+        """b_ptr/x_ptr: device addresses (e.g. torch tensor .data_ptr())."""
+        res = Result()
+        self._check(self.L.gbilu_solve_device(self.h, VP(b_ptr), VP(x_ptr), tol, maxit,
+                                              C.byref(res)))
+        return res
+
+    def solve_host_ptr(self, b_ptr, x_ptr, tol=1e-2, maxit=200):
+        """As solve() on caller-owned (e.g. pinned) host buffers given by address."""
+        res = Result()
+        self._check(self.L.gbilu_solve(self.h, VP(b_ptr), VP(x_ptr), tol, maxit,
+                                       C.byref(res)))
+        return res
+
+    def spmv(self, x, transpose=False):
+        y = np.empty(3 * self.nb)
+        self._check(self.L.gbilu_apply_spmv(self.h, _f64(x), y, int(transpose)))
+        return y
+
+    def ilu_apply(self, p, transpose=False):
+        z = np.empty(3 * self.nb)
+        self._check(self.L.gbilu_apply_ilu(self.h, _f64(p), z, int(transpose)))
+        return z
+
+    def adjoint(self, g, x, tol=1e-10, maxit=2000, want_dA=True):
+        lam = np.empty(3 * self.nb)
+        dA = np.empty(9 * self.nnzb) if want_dA else None
+        res = Result()
+        self._check(self.L.gbilu_adjoint(self.h, _f64(g), _f64(x), lam,
+                                         dA.ctypes.data if want_dA else None, tol, maxit,
+                                         C.byref(res)))
+        return lam, (dA.reshape(-1, 3, 3) if want_dA else None), res
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.gbilu_get_stats(self.h, C.byref(s)))
+        return s.as_dict()
+
+
+def status_string(code):
+    return load().gbilu_status_string(code).decode()

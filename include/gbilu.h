@@ -1,0 +1,184 @@
+/*
+ * gbilu -- GB300-native ILU0-preconditioned BiCGSTAB for 3x3-block BSR
+ * systems. C ABI of libgbilu.so: plain pointers and sizes, int status
+ * returns, caller-owned host arrays, device memory owned by the handle.
+ *
+ * It replaces the host library that drives the OPM/FPGA Alveo kernel
+ * (linearalgebra/ilu0bicgstab/xilinx/src/sda_app/common/
+ * fpga_functions_bicgstab.hpp:30-136). That library consumes a matrix that
+ * the Flow backend has already colored, ILU0-factored and packed; here the
+ * library does those steps itself from plain BSR arrays:
+ *
+ *   fpga_setup_host_datamem (fpga_functions_bicgstab.hpp:33-47)
+ *   + the coloring/packing that fills vectorPointers   -> gbilu_analyze
+ *   fpga_copy_host_datamem (:49-61)
+ *   + fpga_copy_to_device_datamem (:77-78)
+ *   + the ILU0 factorization feeding vectorPointers[18] -> gbilu_factor
+ *   fpga_set_kernel_parameters (:119-122)
+ *   + fpga_kernel_run (:124)
+ *   + fpga_copy_from_device_debugbuf (:84-92)
+ *   + fpga_map_results / fpga_unmap_results (:105-113)  -> gbilu_solve
+ *
+ * Conventions (same as the reference host library):
+ *  - every function returns int, 0 (GBILU_OK) on success; on failure a
+ *    GBILU_* code and a message retrievable with gbilu_last_error();
+ *  - single-threaded use per handle; calls block until the device is done;
+ *  - block values are 3x3 row-major, vals[k*9 + r*3 + c]; vectors hold
+ *    3*nb doubles with unknown 3*i+r belonging to block row i.
+ */
+#ifndef GBILU_H
+#define GBILU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBILU_ABI_VERSION 1
+
+/* return / solve status codes */
+enum {
+  GBILU_OK = 0,                /* converged (solve) or call succeeded */
+  GBILU_MAXIT = 1,             /* stopped at the iteration limit */
+  GBILU_ALREADY_CONVERGED = 2, /* ||b - A x0|| met the bound before any
+                                  iteration; x untouched ("no results",
+                                  bicgstab_utils.cpp:133) */
+  GBILU_BREAKDOWN = 3,         /* (v,rt) == 0, (t,t) == 0 or omega == 0 */
+  GBILU_NONFINITE = 4,         /* NaN or Inf in a residual norm */
+  GBILU_TIMEOUT = 5,           /* device time budget exceeded (the
+                                  reference's abort_cycles,
+                                  fpga_functions_bicgstab.cpp:1254) */
+  GBILU_BAD_INPUT = 6,         /* invalid arguments or sparsity pattern */
+  GBILU_SINGULAR = 7,          /* singular diagonal block in ILU0 */
+  GBILU_CUDA_ERROR = 8,        /* a CUDA call failed */
+  GBILU_NOT_READY = 9,         /* wrong call order (e.g. solve before factor) */
+  GBILU_NO_DEVICE = 10         /* handle created host-only (device = -1) */
+};
+
+/* precision modes */
+enum {
+  GBILU_FP64 = 0,   /* FP64 storage and arithmetic (the reference's mode) */
+  GBILU_MIXED = 1   /* FP32 storage/sweeps inside FP64 iterative refinement */
+};
+
+typedef struct {
+  int precision;      /* GBILU_FP64 or GBILU_MIXED */
+  int absolute_tol;   /* 0: stop when ||r|| <= tol*||r0|| (relative);
+                         1: stop when ||r|| <= tol. Setup-array config bit 1
+                         (fpga_functions_bicgstab.cpp:423, solver.vhd:587) */
+  int device;         /* CUDA device ordinal; -1 = host-only handle that
+                         can analyze and factor but not solve */
+  int use_graph;      /* 1: iteration loop as a CUDA graph with a device-
+                         side while loop; 0: host-driven launches */
+  double timeout_ms;  /* 0 = none; else a solve that exceeds this device
+                         time stops with GBILU_TIMEOUT */
+  double inner_tol;   /* mixed: relative tolerance of each inner solve */
+  int inner_maxit;    /* mixed: iteration limit of each inner solve */
+  int max_outer;      /* mixed: refinement step limit */
+  int verbose;        /* 0 quiet, 1 INFO lines on stdout */
+} gbilu_options;
+
+typedef struct {
+  int status;           /* GBILU_OK, _MAXIT, _ALREADY_CONVERGED, ... */
+  int half_iters;       /* the reference's half-iteration counter at the
+                           stop (bicgstab_utils.cpp:223): 2k after the first
+                           half of iteration k, 2k+1 after the second;
+                           -1 when no iteration ran */
+  double iterations;    /* half_iters/2 + 0.5 (fpga_functions_bicgstab.cpp:926) */
+  double norm0;         /* ||b - A x0|| */
+  double norm;          /* last residual norm the solver computed */
+  double relres;        /* norm / norm0 */
+  double norms[4];      /* norms[0] initial norm, [1..3] ring of the three
+                           latest (bicgstab_utils.cpp:248-258) */
+  int last_norm_idx;    /* index of the newest entry in norms */
+  int outer_iters;      /* mixed: refinement steps taken */
+  int inner_half_iters; /* mixed: inner half-iterations over all steps */
+  double true_relres;   /* mixed: ||b - A x|| / ||b - A x0|| in FP64 */
+  double device_ms;     /* device time of the solve (CUDA events) */
+  double total_ms;      /* host wall time including host<->device copies */
+} gbilu_result;
+
+typedef struct {
+  int nb;               /* block rows */
+  int nnzb;             /* blocks of A */
+  int ncolors;          /* colors of the greedy coloring */
+  int nnzb_lower;       /* blocks of L (strictly lower) */
+  int nnzb_upper;       /* blocks of U (strictly upper) */
+  int slices;           /* 32-row slices of the device layout */
+  long long slots_a;    /* padded block slots of A (x32 lanes) */
+  long long slots_l;
+  long long slots_u;
+  long long device_bytes;   /* device memory held by the handle */
+  int launches_per_iter;    /* kernels one BiCGSTAB iteration launches */
+  long long last_launches;  /* kernels launched by the last solve */
+  double factor_ms;         /* host ILU0 + upload time of the last factor */
+  double analyze_ms;
+} gbilu_stats;
+
+/* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
+ * no timeout, inner_tol 1e-4, inner_maxit 500, max_outer 30 */
+int gbilu_default_options(gbilu_options *opt);
+
+int gbilu_create(const gbilu_options *opt, void **handle);
+int gbilu_destroy(void *handle);
+
+/* Sparsity analysis: greedy block coloring, color-ordered permutation,
+ * L/U split and the device layout. rowptr[nb+1], colind[nnzb] 0-based,
+ * columns sorted and unique per row, diagonal block present.
+ * Structure of fpga_setup_host_datamem's sizes (fpga_functions_bicgstab.cpp
+ * :84-131) and of the coloring that fills vectorPointers (:608-629). */
+int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind);
+
+/* Coloring and ordering chosen by gbilu_analyze; pointers may be NULL.
+ * color[nb], perm[nb] (perm[new] = old), color_ptr[ncolors+1]. */
+int gbilu_get_ordering(void *handle, int *ncolors, int *color, int *perm,
+                       int *color_ptr);
+
+/* Block ILU0 of A (values in the order of the analyzed colind, nnzb*9
+ * doubles) in the color-permuted order, FP64 3x3 inversions, and upload of
+ * A, L, U and the inverted diagonal blocks to the device (the arrays
+ * fpga_copy_host_datamem copies, fpga_functions_bicgstab.cpp:606-629).
+ * Can be called again with new values after one gbilu_analyze. */
+int gbilu_factor(void *handle, const double *vals);
+
+/* The factors computed by gbilu_factor, in the permuted BSR order with
+ * sorted columns (blocks with col < row: L; col >= row: U), and the
+ * inverted diagonal blocks; lu[nnzb*9], dinv[nb*9]; either may be NULL. */
+int gbilu_get_factors(void *handle, double *lu, double *dinv);
+
+/* Solve A x = b. b[3*nb] and x[3*nb] are HOST arrays in the original
+ * numbering; x holds x0 on entry and the solution on return. tol and maxit
+ * follow the reference: maxit full iterations plus the first half of one
+ * more (solver.vhd:557, solver_pkg.vhd:127-128). res may be NULL. */
+int gbilu_solve(void *handle, const double *b, double *x, double tol,
+                int maxit, gbilu_result *res);
+
+/* As gbilu_solve with DEVICE pointers (original numbering). */
+int gbilu_solve_device(void *handle, const double *d_b, double *d_x,
+                       double tol, int maxit, gbilu_result *res);
+
+/* Single operator applications in FP64, host arrays, original numbering:
+ * y = A x (transpose: y = A^T x) -- the SpMV steps 0/4/9 of the PROGRAM
+ * (solver_pkg.vhd:122,126,131); z = (LU)^-1 p (transpose: (LU)^-T p) --
+ * the ILU0 L/U sweeps of steps 2/3 (solver_pkg.vhd:124-125). */
+int gbilu_apply_spmv(void *handle, const double *x, double *y, int transpose);
+int gbilu_apply_ilu(void *handle, const double *p, double *z, int transpose);
+
+/* Adjoint of x = A^-1 b for a loss L(x): given g = dL/dx at the solution
+ * x (host arrays, original numbering), solves A^T lambda = g with the
+ * transposed SpMV and U^T/L^T sweeps reusing the forward factors, and
+ * forms dL/db = lambda and dL/dA = -lambda_i x_j^T on the pattern
+ * (dA[nnzb*9] in the analyzed input block order; may be NULL). No
+ * counterpart in the reference, which has no gradient path. */
+int gbilu_adjoint(void *handle, const double *g, const double *x,
+                  double *lambda, double *dA, double tol, int maxit,
+                  gbilu_result *res);
+
+int gbilu_get_stats(void *handle, gbilu_stats *stats);
+
+const char *gbilu_status_string(int status);
+const char *gbilu_last_error(void *handle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBILU_H */

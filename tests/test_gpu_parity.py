@@ -1,0 +1,176 @@
+"""CUDA path vs the CPU oracle, through the C ABI (libgbilu.so).
+
+Tolerances (norm-wise relative): SpMV and ILU apply 1e-12, solution 1e-6 at
+the same stopping rule, identical half-iteration counts. Sizes are ones the
+oracle finishes in seconds.
+"""
+import numpy as np
+import pytest
+
+from fpga_gb300 import GbIlu
+from fpga_gb300.synth import generate, make_config
+from oracle_lib import Prepared
+
+pytestmark = pytest.mark.gpu
+
+KERNEL_TOL = 1e-12
+SOLUTION_TOL = 1e-6
+
+CASES = {
+    "c1": lambda: make_config("c1_20x20x10"),
+    "faults": lambda: generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7),
+    "sigma2": lambda: generate(24, 24, 10, sigma=2.0, inactive_frac=0.05, fault_frac=0.01, seed=11),
+}
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request, built_lib):
+    s = CASES[request.param]()
+    P = Prepared(s)
+    g = GbIlu(device=0)
+    g.analyze(s.rowptr, s.colind).factor(s.vals)
+    yield s, P, g
+    g.close()
+
+
+def test_ordering_matches_oracle(case):
+    s, P, g = case
+    nc, color, perm, cp = g.ordering()
+    assert nc == P.ncolors
+    assert np.array_equal(color, P.color) and np.array_equal(perm, P.perm)
+    assert np.array_equal(cp, P.color_ptr)
+    lu, dinv = g.factors()
+    assert np.array_equal(lu, P.lu) and np.array_equal(dinv, P.dinv)
+
+
+@pytest.mark.parametrize("transpose", [False, True])
+def test_spmv(case, transpose):
+    s, P, g = case
+    x = np.random.default_rng(1).standard_normal(s.n)
+    assert rel(g.spmv(x, transpose), P.spmv(x, transpose)) < KERNEL_TOL
+
+
+@pytest.mark.parametrize("transpose", [False, True])
+def test_ilu_apply(case, transpose):
+    s, P, g = case
+    p = np.random.default_rng(2).standard_normal(s.n)
+    assert rel(g.ilu_apply(p, transpose), P.ilu_apply(p, transpose)) < KERNEL_TOL
+
+
+@pytest.mark.parametrize("tol", [1e-2, 1e-6])
+def test_solve(case, tol):
+    s, P, g = case
+    x_ref, r_ref = P.solve(s.b, tol=tol, maxit=500)
+    x, r = g.solve(s.b, tol=tol, maxit=500)
+    assert r.status == r_ref.status == 0
+    assert r.half_iters == r_ref.half_iters
+    assert rel(x, x_ref) < SOLUTION_TOL
+    assert abs(r.norm0 - r_ref.norm0) <= 1e-12 * r_ref.norm0
+    assert r.last_norm_idx == r_ref.last_norm_idx
+    true_res = np.linalg.norm(s.b - s.to_scipy() @ x) / np.linalg.norm(s.b)
+    assert true_res <= tol * (1 + 1e-6)
+
+
+def test_graph_and_host_loop_bit_identical(case):
+    s, P, g = case
+    x1, r1 = g.solve(s.b, tol=1e-6, maxit=500)
+    with GbIlu(device=0, use_graph=False) as h:
+        h.analyze(s.rowptr, s.colind).factor(s.vals)
+        x2, r2 = h.solve(s.b, tol=1e-6, maxit=500)
+    assert r1.half_iters == r2.half_iters
+    assert np.array_equal(x1, x2)
+
+
+def test_deterministic(case):
+    s, P, g = case
+    x1, _ = g.solve(s.b, tol=1e-6, maxit=500)
+    x2, _ = g.solve(s.b, tol=1e-6, maxit=500)
+    assert np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("maxit", [0, 1, 2, 3])
+def test_maxit_semantics(case, maxit):
+    s, P, g = case
+    x_ref, r_ref = P.solve(s.b, tol=1e-14, maxit=maxit)
+    x, r = g.solve(s.b, tol=1e-14, maxit=maxit)
+    assert r_ref.status == 1 and r.status == 1
+    assert r.half_iters == r_ref.half_iters == 2 * maxit
+    assert rel(x, x_ref) < 1e-10
+
+
+def test_warm_start(case):
+    s, P, g = case
+    x0 = np.random.default_rng(3).standard_normal(s.n) * 0.1
+    x_ref, r_ref = P.solve(s.b, x0=x0, tol=1e-4, maxit=500)
+    x, r = g.solve(s.b, x0=x0, tol=1e-4, maxit=500)
+    assert r.half_iters == r_ref.half_iters
+    assert rel(x, x_ref) < SOLUTION_TOL
+
+
+def test_already_converged(built_lib):
+    s = make_config("c1_20x20x10")
+    with GbIlu(device=0) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        x0 = np.full(s.n, 7.0)
+        x, r = g.solve(np.zeros(s.n), x0=np.zeros(s.n), tol=1e-2)
+        assert r.status == 2 and r.half_iters == -1
+        # x untouched when no iteration ran
+        b = s.to_scipy() @ x0
+        x, r = g.solve(b, x0=x0, tol=1e-2)
+        assert r.status == 2 and np.array_equal(x, x0)
+
+
+def test_absolute_tolerance(built_lib):
+    s = make_config("c1_20x20x10")
+    P = Prepared(s)
+    x_ref, r_ref = P.solve(s.b, tol=1.0, maxit=200, absolute=True)
+    with GbIlu(device=0, absolute=True) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        x, r = g.solve(s.b, tol=1.0, maxit=200)
+        assert r.status == 0 and r.norm <= 1.0
+        assert r.half_iters == r_ref.half_iters
+        assert rel(x, x_ref) < SOLUTION_TOL
+        x, r = g.solve(s.b, tol=1e6, maxit=200)   # ||r0|| below the absolute bound
+        assert r.status == 2
+
+
+def test_nonfinite_rhs(built_lib):
+    s = make_config("c1_20x20x10")
+    with GbIlu(device=0) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        b = s.b.copy()
+        b[17] = np.nan
+        x, r = g.solve(b, tol=1e-2)
+        assert r.status == 4
+        # the handle stays usable
+        x, r = g.solve(s.b, tol=1e-2)
+        assert r.status == 0
+
+
+def test_timeout_status(built_lib):
+    s = generate(40, 40, 20, sigma=2.0, seed=5)
+    with GbIlu(device=0, timeout_ms=1e-3) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        x, r = g.solve(s.b, tol=1e-14, maxit=100000)
+        assert r.status == 5
+        x, r = g.solve(s.b, tol=1e-2, maxit=100)
+        assert r.status in (0, 5)
+
+
+def test_config2_size_properties(built_lib):
+    """Full 500k-cell system: SpMV parity and the 1e-2 solve against the oracle."""
+    s = make_config("c2_100x100x50")
+    P = Prepared(s)
+    with GbIlu(device=0) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        x = np.random.default_rng(4).standard_normal(s.n)
+        assert rel(g.spmv(x), P.spmv(x)) < KERNEL_TOL
+        assert rel(g.ilu_apply(x), P.ilu_apply(x)) < KERNEL_TOL
+        xs, r = g.solve(s.b, tol=1e-2, maxit=1000)
+        xr, rr = P.solve(s.b, tol=1e-2, maxit=1000)
+        assert r.half_iters == rr.half_iters and r.status == 0
+        assert rel(xs, xr) < SOLUTION_TOL
