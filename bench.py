@@ -1,0 +1,368 @@
+"""Benchmark of the GB300 ILU0-BiCGSTAB solve (one JSON line on rank 0).
+
+Metric: ILU0-BiCGSTAB solve time on the 100x100x50 (500k-cell, 1.425M
+unknowns) system at relative residual 1e-2, FP64 (``value``, ms per solve,
+inputs resident in HBM), the same through the host-buffer C-ABI call
+(``e2e``), the mixed-precision form against FP64 at 1e-8 on the sigma=2.0
+system, and the adjoint/forward time ratio on the 60x60x30 system.
+
+A "step" is one solve of the 500k-cell system from x0 = 0. Inputs are larger
+than L2 (the matrix values alone are 0.23 GB), so no L2 flush is inserted.
+``--impl reference`` times the CPU restatement of the same algorithm (the
+reference has no CPU solver; its arithmetic exists only as FPGA RTL) on all
+host cores.
+
+Multi-GPU: the solve does not shard without changing the preconditioner, so
+N > 1 runs N independent replicas (one system per rank, seeded by rank),
+value = max-over-ranks time / (K * N).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ILU0-BiCGSTAB solve ms @relres 1e-2: FP64 vs mixed; HBM GB/s; adjoint/fwd"
+WORKLOAD = "c2_100x100x50"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f".clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+            os.remove(self.path)
+        except Exception:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if len(r) >= 9]
+        mx = [float(r[2]) for r in rows if len(r) >= 9]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4)
+                          if r[5 + i].strip().lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            import torch
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cpu" if dist.get_backend() == "gloo" else f"cuda:{torch.cuda.current_device()}"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_reference(args, world, rank):
+    """The reference arm: the CPU restatement (oracle) on all host cores."""
+    if rank != 0:
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Prepared
+    from fpga_gb300.synth import make_config, CONFIGS
+    cores = os.cpu_count() or 1
+    s = make_config(WORKLOAD)
+    P = Prepared(s)
+    tol = CONFIGS[WORKLOAD]["tol"]
+    for _ in range(max(1, args.warmup)):
+        P.solve_omp(s.b, tol=tol, maxit=1000, nthreads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        x, r = P.solve_omp(s.b, tol=tol, maxit=1000, nthreads=cores)
+        times.append((time.perf_counter() - t0) * 1e3)
+    ms = statistics.mean(times)
+    out = {"impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded generator, no dataset)",
+           "config": {"workload": WORKLOAD, "grid": [100, 100, 50], "nb": s.nb, "tol": tol,
+                      "half_iters": r.half_iters, "relres": r.relres},
+           "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
+                            "sample": f"{args.steps} full solves of {WORKLOAD} to relres {tol} "
+                                      "(OpenMP C restatement of the reference algorithm)"},
+           "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def gpu_bench(args, world, rank, local):
+    import numpy as np
+    import torch
+    from fpga_gb300 import GbIlu
+    from fpga_gb300.synth import make_config, generate, CONFIGS, adjoint_selection
+
+    torch.cuda.set_device(local)
+    cfg = CONFIGS[WORKLOAD]
+    s = make_config(WORKLOAD, seed=rank)
+    tol, maxit = cfg["tol"], cfg["maxit"]
+    g = GbIlu(device=local, precision="mixed")
+    g.analyze(s.rowptr, s.colind).factor(s.vals)
+    st = g.stats()
+    n = s.n
+    b_dev = torch.from_numpy(s.b).to(f"cuda:{local}")
+    x_dev = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
+    # FP64 run on device pointers: warm-up, then K timed solves
+    g64 = GbIlu(device=local, precision="fp64")
+    g64.analyze(s.rowptr, s.colind).factor(s.vals)
+    for _ in range(args.warmup):
+        x_dev.zero_()
+        g64.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), tol, maxit)
+    torch.cuda.synchronize()
+    res = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_ms = 0.0
+        for _ in range(args.steps):
+            x_dev.zero_()
+            r = g64.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), tol, maxit)
+            res.append(r)
+            dev_ms += r.device_ms
+            launches += g64.stats()["last_launches"]
+        torch.cuda.synchronize()
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        barrier(world)
+    clocks = clk.summary()
+    # device time of the solves (CUDA events on the library's stream), max over ranks
+    ms_step = barrier_max(world, dev_ms / args.steps)
+    value = ms_step / world
+    r0 = res[-1]
+    x_np = x_dev.cpu().numpy()
+    true_relres = float(np.linalg.norm(s.b - s.to_scipy() @ x_np) / np.linalg.norm(s.b))
+
+    # e2e: host pinned buffers through gbilu_solve (H2D b, x0; D2H x inside)
+    b_pin = torch.from_numpy(s.b).pin_memory()
+    x_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        x_pin.zero_()
+        g64.solve_host_ptr(b_pin.data_ptr(), x_pin.data_ptr(), tol, maxit)
+    e2e_ms = []
+    for _ in range(args.steps):
+        x_pin.zero_()
+        t0 = time.perf_counter()
+        g64.solve_host_ptr(b_pin.data_ptr(), x_pin.data_ptr(), tol, maxit)
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = barrier_max(world, statistics.mean(e2e_ms)) / world
+
+    # dominant-kernel roofline: kernels timed back to back with CUDA events
+    peak, peak_kind = peaks()
+    kern = {}
+    for name in ("spmv64", "ilu64", "spmv32", "ilu32"):
+        ms, by, la = g.bench_kernel(name, reps=20)
+        kern[name] = {"ms": ms, "alg_bytes": by, "launches": la, "gbs": by / ms / 1e6}
+    it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
+    solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "spmv64_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+    dom = kern["spmv64"]
+    roofline = {"bound": "hbm", "kernel": "k_spmv<double> (BSR3 SpMV, FP64)",
+                "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": dom["gbs"] / peak, "traffic": traffic,
+                "peak_kind": peak_kind, "alg_bytes_per_launch": dom["alg_bytes"]}
+
+    extra = {}
+    if not args.quick and rank == 0:
+        extra = secondary(args, local, tol)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.quick:
+        cpu = cpu_baseline(s, tol, maxit)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+               "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic (seeded generator, no dataset)",
+               "config": {"workload": WORKLOAD, "grid": [100, 100, 50], "nb": s.nb,
+                          "nnzb": st["nnzb"], "colors": st["ncolors"], "tol": tol,
+                          "sigma": cfg["sigma"], "inactive": cfg["inactive"],
+                          "faults": cfg["faults"], "x0": "zero",
+                          "l2": "inputs larger than L2 (FP64 A 0.23 GB, L+U 0.19 GB)",
+                          "parallelism": f"replicas{world}" if world > 1 else "single"},
+               "result": {"status": r0.status, "half_iters": r0.half_iters,
+                          "relres": r0.relres, "true_relres": true_relres},
+               "wall_ms_per_step": wall_ms / args.steps,
+               "solve_gbs": solve_gbs,
+               "solve_frac_of_peak": solve_gbs / peak if solve_gbs else None,
+               "kernels": kern,
+               "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": 2 * n * 8,
+                       "d2h_bytes_per_step": n * 8},
+               "gpu_launches": int(launches),
+               "roofline": roofline,
+               "clocks": clocks}
+        out.update(extra)
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+
+
+def cpu_baseline(s, tol, maxit):
+    """The oracle's OpenMP solver on the host cores, a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Prepared
+    cores = os.cpu_count() or 1
+    P = Prepared(s)
+    P.solve_omp(s.b, tol=tol, maxit=maxit, nthreads=cores)
+    times = []
+    t_end = time.perf_counter() + 10.0
+    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 20):
+        t0 = time.perf_counter()
+        P.solve_omp(s.b, tol=tol, maxit=maxit, nthreads=cores)
+        times.append((time.perf_counter() - t0) * 1e3)
+    return {"value": statistics.median(times), "unit": "ms", "cores": cores, "kind": "port",
+            "sample": f"{len(times)} full solves of {WORKLOAD} to relres {tol} "
+                      "(median; OpenMP C restatement, oracle/gbilu_oracle.c)"}
+
+
+def secondary(args, local, tol64):
+    """Mixed vs FP64 at 1e-8 (sigma=2.0 system) and adjoint/forward ratio."""
+    import numpy as np
+    from fpga_gb300 import GbIlu
+    from fpga_gb300.synth import make_config, CONFIGS, adjoint_selection
+    out = {}
+    c3 = CONFIGS["c3_100x100x50_mixed"]
+    s = make_config("c3_100x100x50_mixed")
+    tol = c3["tol"]
+    times = {}
+    sols = {}
+    for prec in ("fp64", "mixed"):
+        g = GbIlu(device=local, precision=prec)
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        g.solve(s.b, tol=tol, maxit=c3["maxit"])
+        ms = []
+        for _ in range(3):
+            x, r = g.solve(s.b, tol=tol, maxit=c3["maxit"])
+            ms.append(r.device_ms)
+        times[prec] = (statistics.median(ms), r)
+        sols[prec] = x
+        g.close()
+    A = s.to_scipy()
+    err = float(np.linalg.norm(sols["mixed"] - sols["fp64"]) / np.linalg.norm(sols["fp64"]))
+    tr = {p: float(np.linalg.norm(s.b - A @ sols[p]) / np.linalg.norm(s.b)) for p in sols}
+    out["mixed"] = {"workload": "c3_100x100x50_mixed (sigma=2.0)", "tol": tol,
+                    "fp64_ms": times["fp64"][0], "mixed_ms": times["mixed"][0],
+                    "speedup": times["fp64"][0] / times["mixed"][0],
+                    "fp64_half_iters": times["fp64"][1].half_iters,
+                    "mixed_outer": times["mixed"][1].outer_iters,
+                    "mixed_inner_half_iters": times["mixed"][1].inner_half_iters,
+                    "true_relres": tr, "x_err_vs_fp64": err}
+    # adjoint / forward on the 60x60x30 system
+    c4 = CONFIGS["c4_60x60x30_adjoint"]
+    s = make_config("c4_60x60x30_adjoint")
+    g = GbIlu(device=local, precision="fp64")
+    g.analyze(s.rowptr, s.colind).factor(s.vals)
+    cells, d = adjoint_selection(s.nb)
+    idx = (3 * cells[:, None] + np.arange(3)).reshape(-1)
+    x, r = g.solve(s.b, tol=c4["tol"], maxit=c4["maxit"])
+    fw, bw = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        x, r = g.solve(s.b, tol=c4["tol"], maxit=c4["maxit"])
+        fw.append(r.device_ms)
+        gvec = np.zeros(s.n)
+        gvec[idx] = x[idx] - d
+        lam, dA, ra = g.adjoint(gvec, x, tol=c4["tol"], maxit=c4["maxit"])
+        bw.append(ra.device_ms)
+    out["adjoint"] = {"workload": "c4_60x60x30_adjoint", "tol": c4["tol"],
+                      "forward_ms": statistics.median(fw), "adjoint_ms": statistics.median(bw),
+                      "ratio": statistics.median(bw) / statistics.median(fw),
+                      "forward_half_iters": r.half_iters, "adjoint_half_iters": ra.half_iters}
+    g.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--quick", action="store_true",
+                    help="only the FP64 500k-cell solve (for profiler runs)")
+    args = ap.parse_args()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        cpu_reference(args, world, rank)
+    else:
+        gpu_bench(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -805,6 +805,78 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   s->last_launches = h->last_launches;
   s->factor_ms = h->factor_ms;
   s->analyze_ms = h->analyze_ms;
+  for (int p = 0; p < 2; ++p) {
+    const double sv = p ? 4.0 : 8.0, sx = sv, si = 4.0;
+    const double nb = an.nb, n = 3.0 * an.nb, n0 = first_color_unknowns(h, false);
+    const double nlu = (double)an.nnzb_l + an.nnzb_u;
+    s->alg_bytes_spmv[p] = an.nnzb * (9 * sv + si) + (nb + 1) * si + 2 * n * sx;
+    s->alg_bytes_ilu[p] = nlu * (9 * sv + si) + 2 * (nb + 1) * si + nb * 9 * sv + 4 * n * sx;
+    // fused vector kernels of one iteration: update_s (r, v -> s, s^[c0]),
+    // update_r (x, p^, s^, s, t, rt -> x, r), update_p (r, v, p -> p, p^[c0])
+    // and the dot operands of the two SpMV epilogues (rt, s)
+    const double vec = (17.0 * n + 2.0 * n0) * sx;
+    s->alg_bytes_iter[p] = 2 * s->alg_bytes_spmv[p] + 2 * s->alg_bytes_ilu[p] + vec;
+  }
+  return GBILU_OK;
+}
+
+int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double *alg_bytes,
+                       int *launches_out) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  if (which < 0 || which > 3 || reps <= 0) return h->fail(GBILU_BAD_INPUT, "bad kernel id or reps");
+  if (which >= 2 && !h->with_32) return h->fail(GBILU_BAD_INPUT, "FP32 kernels need GBILU_MIXED");
+  CK(cudaSetDevice(h->opt.device));
+  gbilu_stats st;
+  gbilu_get_stats(h, &st);
+  const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
+  const int n0 = first_color_unknowns(h, false);
+  int launches = 0;
+  k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
+  // inputs: a fixed pseudo-random vector in the permuted numbering
+  std::vector<double> x(n);
+  uint64_t z = 0x9e3779b97f4a7c15ull;
+  for (int i = 0; i < n; ++i) {
+    z ^= z << 13; z ^= z >> 7; z ^= z << 17;
+    x[i] = (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+  }
+  CK(cudaMemcpyAsync(h->v64.p.p, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  if (h->with_32) k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0, h->v64.p.p, h->v32.p.p);
+  if (n0) {
+    CK(cudaMemcpyAsync(h->v64.ph.p, h->v64.p.p, n0 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    if (h->with_32)
+      CK(cudaMemcpyAsync(h->v32.ph.p, h->v32.p.p, n0 * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+  }
+  auto run = [&](int &l) {
+    if (which == 0) {
+      Ops<double, double> o = make_ops<double, double>(h, false);
+      spmv<double, double, SPMV_PLAIN>(h, h->st, o, h->v64.p.p, h->v64.v.p, nullptr, l);
+    } else if (which == 1) {
+      Ops<double, double> o = make_ops<double, double>(h, false);
+      apply_prec(h, h->st, o, h->v64.p.p, h->v64.ph.p, l);
+    } else if (which == 2) {
+      Ops<float, float> o = make_ops<float, float>(h, false);
+      spmv<float, float, SPMV_PLAIN>(h, h->st, o, h->v32.p.p, h->v32.v.p, nullptr, l);
+    } else {
+      Ops<float, float> o = make_ops<float, float>(h, false);
+      apply_prec(h, h->st, o, h->v32.p.p, h->v32.ph.p, l);
+    }
+  };
+  int warm = 0;
+  for (int i = 0; i < 3; ++i) run(warm);
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaEventRecord(h->e0, h->st));
+  for (int i = 0; i < reps; ++i) run(launches);
+  CK(cudaEventRecord(h->e1, h->st));
+  CK(cudaEventSynchronize(h->e1));
+  CK(cudaGetLastError());
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->e0, h->e1));
+  if (avg_ms) *avg_ms = ms / reps;
+  if (alg_bytes) *alg_bytes = (which == 0 || which == 2) ? st.alg_bytes_spmv[which / 2] : st.alg_bytes_ilu[which / 2];
+  if (launches_out) *launches_out = launches / reps;
   return GBILU_OK;
 }
 

@@ -48,10 +48,15 @@ class Stats(C.Structure):
                 ("slots_a", C.c_longlong), ("slots_l", C.c_longlong),
                 ("slots_u", C.c_longlong), ("device_bytes", C.c_longlong),
                 ("launches_per_iter", C.c_int), ("last_launches", C.c_longlong),
-                ("factor_ms", C.c_double), ("analyze_ms", C.c_double)]
+                ("factor_ms", C.c_double), ("analyze_ms", C.c_double),
+                ("alg_bytes_spmv", C.c_double * 2), ("alg_bytes_ilu", C.c_double * 2),
+                ("alg_bytes_iter", C.c_double * 2)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        for k in ("alg_bytes_spmv", "alg_bytes_ilu", "alg_bytes_iter"):
+            d[k] = list(d[k])
+        return d
 
 
 class GbIluError(RuntimeError):
@@ -95,6 +100,8 @@ def load():
     L.gbilu_adjoint.argtypes = [VP, F64P, F64P, F64P, VP, C.c_double, C.c_int,
                                 C.POINTER(Result)]
     L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
+    L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.gbilu_status_string.argtypes = [C.c_int]
     L.gbilu_status_string.restype = C.c_char_p
     L.gbilu_last_error.argtypes = [VP]
@@ -168,7 +175,7 @@ class GbIlu:
 
     def factor(self, vals):
         v = _f64(vals).reshape(-1)
-        if v.size != 9 * self.nnzb:
+        if self.nb and v.size != 9 * self.nnzb:
             raise ValueError("vals must hold nnzb*9 doubles")
         self._check(self.L.gbilu_factor(self.h, v))
         return self
@@ -235,6 +242,15 @@ class GbIlu:
         s = Stats()
         self._check(self.L.gbilu_get_stats(self.h, C.byref(s)))
         return s.as_dict()
+
+    KERNELS = {"spmv64": 0, "ilu64": 1, "spmv32": 2, "ilu32": 3}
+
+    def bench_kernel(self, which, reps=20):
+        """(avg ms, algorithmic bytes, launches) per application of a kernel family."""
+        ms, by, la = C.c_double(), C.c_double(), C.c_int()
+        self._check(self.L.gbilu_bench_kernel(self.h, self.KERNELS[which], reps, C.byref(ms),
+                                               C.byref(by), C.byref(la)))
+        return ms.value, by.value, la.value
 
 
 def status_string(code):

@@ -112,6 +112,12 @@ typedef struct {
   long long last_launches;  /* kernels launched by the last solve */
   double factor_ms;         /* host ILU0 + upload time of the last factor */
   double analyze_ms;
+  /* algorithmic bytes (every operand read or written once, x gathers
+   * counted once) of one SpMV, one ILU apply and one full iteration:
+   * [0] FP64 storage and vectors, [1] FP32 storage and vectors */
+  double alg_bytes_spmv[2];
+  double alg_bytes_ilu[2];
+  double alg_bytes_iter[2];
 } gbilu_stats;
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
@@ -174,6 +180,16 @@ int gbilu_adjoint(void *handle, const double *g, const double *x,
                   gbilu_result *res);
 
 int gbilu_get_stats(void *handle, gbilu_stats *stats);
+
+/* Times one kernel family on the handle's stream with CUDA events, reps
+ * applications back to back on the factored system: which = 0 SpMV FP64,
+ * 1 ILU apply FP64 (all colors), 2 SpMV FP32, 3 ILU apply FP32 (2/3 need
+ * GBILU_MIXED). Returns the average device ms per application, its
+ * algorithmic bytes and the kernel launches per application. The
+ * counterpart of the reference's kernel timing around clEnqueueTask
+ * (fpga_functions_bicgstab.cpp:1305-1325), per kernel instead of per run. */
+int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
+                       double *alg_bytes, int *launches);
 
 const char *gbilu_status_string(int status);
 const char *gbilu_last_error(void *handle);

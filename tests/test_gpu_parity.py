@@ -115,12 +115,15 @@ def test_already_converged(built_lib):
     s = make_config("c1_20x20x10")
     with GbIlu(device=0) as g:
         g.analyze(s.rowptr, s.colind).factor(s.vals)
-        x0 = np.full(s.n, 7.0)
+        # ||r0|| = 0 <= 1e-30: "no results", no iteration
         x, r = g.solve(np.zeros(s.n), x0=np.zeros(s.n), tol=1e-2)
-        assert r.status == 2 and r.half_iters == -1
+        assert r.status == 2 and r.half_iters == -1 and r.norm0 == 0.0
+    with GbIlu(device=0, absolute=True) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
         # x untouched when no iteration ran
-        b = s.to_scipy() @ x0
-        x, r = g.solve(b, x0=x0, tol=1e-2)
+        x0 = np.full(s.n, 7.0)
+        b = s.to_scipy() @ x0 + 1e-9
+        x, r = g.solve(b, x0=x0, tol=1e-3)
         assert r.status == 2 and np.array_equal(x, x0)
 
 

@@ -1,0 +1,84 @@
+"""libgbilu.so on the CPU: it loads, exports what include/gbilu.h declares,
+and its host-side analysis (coloring, permutation, ILU0 factors) matches the
+oracle bit for bit. Host-only handles (device = -1) make no CUDA call."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from fpga_gb300 import GbIlu, GbIluError, native
+from fpga_gb300.synth import generate, make_config
+from oracle_lib import Prepared
+
+CASES = {
+    "c1": lambda: make_config("c1_20x20x10"),
+    "faults": lambda: generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7),
+    "single": lambda: generate(1, 1, 1, seed=0),
+    "line": lambda: generate(17, 1, 1, seed=1),
+}
+
+
+def test_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(built_lib)
+    names = native.declared_symbols()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_host_analysis_matches_oracle(built_lib, name):
+    s = CASES[name]()
+    P = Prepared(s)
+    with GbIlu(device=-1) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        nc, color, perm, cp = g.ordering()
+        assert nc == P.ncolors
+        assert np.array_equal(color, P.color)
+        assert np.array_equal(perm, P.perm)
+        assert np.array_equal(cp, P.color_ptr)
+        lu, dinv = g.factors()
+        assert np.array_equal(lu, P.lu)
+        assert np.array_equal(dinv, P.dinv)
+        st = g.stats()
+        assert st["nnzb_lower"] + st["nnzb_upper"] + st["nb"] == st["nnzb"]
+        assert st["slots_a"] * 32 >= st["nnzb"]
+
+
+def expect(code, fn, *a):
+    with pytest.raises(GbIluError) as e:
+        fn(*a)
+    assert e.value.code == code, str(e.value)
+
+
+def test_error_behaviour(built_lib):
+    s = make_config("c1_20x20x10")
+    with GbIlu(device=-1) as g:
+        expect(native.NOT_READY, g.factor, s.vals)            # factor before analyze
+        bad = s.colind.copy()
+        bad[[0, 1]] = bad[[1, 0]]                              # unsorted row 0
+        expect(native.BAD_INPUT, g.analyze, s.rowptr, bad)
+        bad = s.colind.copy()
+        bad[5] = s.nb + 3                                      # out of range
+        expect(native.BAD_INPUT, g.analyze, s.rowptr, bad)
+        rp = s.rowptr.copy()
+        rp[0] = 1
+        expect(native.BAD_INPUT, g.analyze, rp, s.colind)
+        # a row without its diagonal block
+        keep = np.ones(s.nnzb, bool)
+        keep[np.nonzero(s.colind[s.rowptr[3]:s.rowptr[4]] == 3)[0][0] + s.rowptr[3]] = False
+        rp = np.concatenate([[0], np.cumsum([keep[s.rowptr[i]:s.rowptr[i + 1]].sum() for i in range(s.nb)])])
+        expect(native.BAD_INPUT, g.analyze, rp, s.colind[keep])
+        g.analyze(s.rowptr, s.colind)
+        vals = s.vals.copy()
+        d = np.nonzero(s.colind[s.rowptr[10]:s.rowptr[11]] == 10)[0][0] + s.rowptr[10]
+        vals[d] = 0.0                                          # singular pivot
+        expect(native.SINGULAR, g.factor, vals)
+        g.factor(s.vals)
+        expect(native.NO_DEVICE, g.solve, s.b)                 # host-only handle
+
+
+def test_status_strings(built_lib):
+    for code in range(11):
+        assert native.status_string(code) != "unknown status"
