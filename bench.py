@@ -169,7 +169,7 @@ def gpu_bench(args, world, rank, local):
     b_dev = torch.from_numpy(s.b).to(f"cuda:{local}")
     x_dev = torch.zeros(n, dtype=torch.float64, device=f"cuda:{local}")
     # FP64 run on device pointers: warm-up, then K timed solves
-    g64 = GbIlu(device=local, precision="fp64")
+    g64 = GbIlu(device=local, precision="fp64", use_graph=not args.no_graph)
     g64.analyze(s.rowptr, s.colind).factor(s.vals)
     for _ in range(args.warmup):
         x_dev.zero_()
@@ -353,6 +353,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--quick", action="store_true",
                     help="only the FP64 500k-cell solve (for profiler runs)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven launches instead of the graph loop (profiler runs: "
+                         "kernels inside a conditional graph node are not listed by ncu)")
     args = ap.parse_args()
     world, rank, local = dist_init(args)
     if args.impl == "reference":

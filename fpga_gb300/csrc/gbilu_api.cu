@@ -92,6 +92,8 @@ struct Handle {
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][transpose]
   int per_iter[2] = {0, 0};                // launches per iteration [transpose]
   long long last_launches = 0;
+  PhaseList phases[2];                     // color steps [transpose]
+  int coop_grid64 = 1, coop_grid32 = 1;    // CTAs of the cooperative apply
   size_t device_bytes = 0;
 
   int fail(int code, const char *fmt, ...) {
@@ -137,12 +139,67 @@ void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, cons
   ++launches;
 }
 
+// The color steps of one preconditioner apply, in execution order.
+PhaseList make_phases(const Analysis &an, bool transpose) {
+  PhaseList pl;
+  pl.n = 0;
+  const int C = an.ncolors;
+  auto add = [&](int c, int mat, int has_d) {
+    Phase &p = pl.p[pl.n++];
+    p.row0 = an.color_ptr[c];
+    p.nrows = an.color_ptr[c + 1] - an.color_ptr[c];
+    p.slice0 = an.slice_color_ptr[c];
+    p.mat = mat;
+    p.has_d = has_d;
+  };
+  if (!transpose) {
+    if (C == 1) {
+      add(0, 0, 1);
+    } else {
+      for (int c = 1; c < C; ++c) add(c, 0, c == C - 1);
+      for (int c = C - 2; c >= 0; --c) add(c, 1, 1);
+    }
+  } else {
+    for (int c = 0; c < C; ++c) add(c, 0, 1);
+    for (int c = C - 2; c >= 0; --c) add(c, 1, 0);
+  }
+  return pl;
+}
+
+template <typename V, typename T>
+int coop_grid(Handle *h) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kThreads, 0);
+  int most = 0;
+  for (int c = 0; c < h->an.ncolors; ++c)
+    most = std::max(most, h->an.color_ptr[c + 1] - h->an.color_ptr[c]);
+  const int need = (most + kThreads - 1) / kThreads;
+  return std::max(1, std::min(per_sm * h->sm_count, need));
+}
+
 // hat = M^-1 src (forward) or M^-T src (transpose). In the forward case with
 // two or more colors, hat must already hold src on color 0's unknowns.
 template <typename V, typename T>
 void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *hat,
                 int &launches) {
   const int C = h->an.ncolors;
+  if (h->opt.sweep_mode == 1 && C <= kMaxPhases / 2) {
+    const PhaseList &pl = h->phases[o.transpose ? 1 : 0];
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.gridDim = dim3(sizeof(T) == 8 ? h->coop_grid64 : h->coop_grid32);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, o.off1, o.col1, o.val1, o.off2,
+                       o.col2, o.val2, o.dmat, src, hat);
+    ++launches;
+    return;
+  }
   if (!o.transpose) {
     if (C == 1) {
       sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, 0, src, hat, hat, launches);
@@ -402,6 +459,10 @@ int setup_device(Handle *h) {
   const size_t maxgrid = std::max<size_t>((size_t)h->sm_count * 8, (size_t)(an.S + kWarps - 1) / kWarps) + 1;
   CK(h->partials.alloc(2 * maxgrid));
   CK(h->ctl.alloc(2));
+  h->phases[0] = make_phases(an, false);
+  h->phases[1] = make_phases(an, true);
+  h->coop_grid64 = coop_grid<double, double>(h);
+  h->coop_grid32 = coop_grid<float, float>(h);
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
                      (size_t)an.nnzb * 8 + (size_t)an.nb * 8;
   return GBILU_OK;
@@ -432,6 +493,7 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   out = *h->h_ctl;
+  if (h->opt.use_graph) launches += (long long)out.body_runs * h->per_iter[transpose ? 1 : 0];
   return GBILU_OK;
 }
 
@@ -487,6 +549,7 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
     CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     const Ctl ic = *h->h_ctl;
+    if (h->opt.use_graph) launches += (long long)ic.body_runs * h->per_iter[transpose ? 1 : 0];
     inner_half += (ic.half >= 0 ? ic.half + 1 : 0);
     ++outer_steps;
     if (ic.status == ST_BREAKDOWN || ic.status == ST_NONFINITE) { out.status = ic.status; break; }
@@ -530,6 +593,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->inner_maxit = 500;
   o->max_outer = 30;
   o->verbose = 0;
+  o->sweep_mode = 1;
   return GBILU_OK;
 }
 

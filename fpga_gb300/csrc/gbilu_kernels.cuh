@@ -40,6 +40,9 @@ struct Ctl {
   int done, status, stop_half;    // stop_half: stopped after a first half
   unsigned long long t_start, timeout_ns;
   unsigned int counter[8];        // arrival counters of the last-block pattern
+  unsigned int bar_count, bar_gen;  // grid barrier of cooperative launches
+  int bar_fail;                   // a barrier wait timed out
+  int body_runs;                  // loop bodies run (graph launches count)
 };
 
 // --------------------------------------------------------------------------
@@ -172,6 +175,10 @@ __global__ void k_ctl_init(Ctl *c, double tol, int absolute, int maxit,
     c->t_start = globaltimer();
     c->timeout_ns = timeout_ns;
     for (int i = 0; i < 8; ++i) c->counter[i] = 0u;
+    c->bar_count = 0u;
+    c->bar_gen = 0u;
+    c->bar_fail = 0;
+    c->body_runs = 0;
   }
 }
 
@@ -197,6 +204,61 @@ __device__ __forceinline__ void finish_init(Ctl *c, double rr) {
 }
 
 // --------------------------------------------------------------------------
+// one sliced row: a += sign * sum_k B_k x_{c_k}
+// --------------------------------------------------------------------------
+
+constexpr int kBatch = 4;   // blocks whose loads are in flight together
+
+// Loads of vectors that other CTAs of the same kernel wrote go through L2
+// (ld.global.cg): the per-SM L1 is not coherent inside one launch.
+template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p) {
+  if (CG) return __ldcg(p);
+  return *p;
+}
+
+// Column indices are fetched kBatch at a time, so the gathers and the 9
+// coalesced value loads of kBatch blocks are in flight together: a row of
+// w blocks costs about 2*ceil(w/kBatch) memory round trips instead of 2*w.
+// Padding slots (column -1) only occur after a row's last block.
+template <typename V, typename T, bool NEG, bool CG>
+__device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V *__restrict__ val,
+                                           int o, int wdt, int lane, const T *x, T &a0, T &a1,
+                                           T &a2) {
+  for (int k0 = 0; k0 < wdt; k0 += kBatch) {
+    int c[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j)
+      c[j] = (k0 + j < wdt) ? ldg_stream(col + (size_t)(o + k0 + j) * 32 + lane) : -1;
+    // all loads of the batch first ...
+    T xv[kBatch][3];
+    V b[kBatch][9];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      if (c[j] >= 0) {
+        const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) xv[j][e] = ldv<CG>(x + 3 * c[j] + e);
+#pragma unroll
+        for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
+      }
+    }
+    // ... then the multiply-adds
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      if (c[j] >= 0) {
+        T bb[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) bb[e] = NEG ? -(T)b[j][e] : (T)b[j][e];
+        a0 = fma(bb[0], xv[j][0], a0); a0 = fma(bb[1], xv[j][1], a0); a0 = fma(bb[2], xv[j][2], a0);
+        a1 = fma(bb[3], xv[j][0], a1); a1 = fma(bb[4], xv[j][1], a1); a1 = fma(bb[5], xv[j][2], a1);
+        a2 = fma(bb[6], xv[j][0], a2); a2 = fma(bb[7], xv[j][1], a2); a2 = fma(bb[8], xv[j][2], a2);
+      }
+    }
+    if (c[kBatch - 1] < 0) break;
+  }
+}
+
+// --------------------------------------------------------------------------
 // sliced SpMV with fused reductions
 // --------------------------------------------------------------------------
 
@@ -206,7 +268,7 @@ enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3 }
 // (y, w) -> alpha = rho/(y,w) (step 5). OMEGA: (y, w), (y, y) ->
 // omega = (y,w)/(y,y) (step 10). V: matrix value type, T: vector type.
 template <typename V, typename T, int MODE>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
        T *__restrict__ y, const T *__restrict__ w, double *partials) {
@@ -221,22 +283,7 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
       const int row = sr.x + lane;
       const int o = off[s], wdt = off[s + 1] - o;
       T a0 = 0, a1 = 0, a2 = 0;
-      for (int k = 0; k < wdt; ++k) {
-        const size_t slot = (size_t)(o + k);
-        const int c = ldg_stream(col + slot * 32 + lane);
-        if (c < 0) break;
-        const T x0 = x[3 * c], x1 = x[3 * c + 1], x2 = x[3 * c + 2];
-        const V *v = val + slot * 9 * 32 + lane;
-        a0 = fma((T)ldg_stream(v + 0 * 32), x0, a0);
-        a0 = fma((T)ldg_stream(v + 1 * 32), x1, a0);
-        a0 = fma((T)ldg_stream(v + 2 * 32), x2, a0);
-        a1 = fma((T)ldg_stream(v + 3 * 32), x0, a1);
-        a1 = fma((T)ldg_stream(v + 4 * 32), x1, a1);
-        a1 = fma((T)ldg_stream(v + 5 * 32), x2, a1);
-        a2 = fma((T)ldg_stream(v + 6 * 32), x0, a2);
-        a2 = fma((T)ldg_stream(v + 7 * 32), x1, a2);
-        a2 = fma((T)ldg_stream(v + 8 * 32), x2, a2);
-      }
+      row_blocks<V, T, false, false>(col, val, o, wdt, lane, x, a0, a1, a2);
       if (MODE == SPMV_RESID) {
         a0 = w[3 * row] - a0; a1 = w[3 * row + 1] - a1; a2 = w[3 * row + 2] - a2;
       }
@@ -287,47 +334,121 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
 // one color of a triangular sweep
 // --------------------------------------------------------------------------
 
-// dst_i = [D_i] (src_i - sum_j B_ij nbr_j) for the rows of one color.
+// One row of a sweep: dst_i = [D_i] (src_i - sum_j B_ij nbr_j).
+template <typename V, typename T, bool CG>
+__device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *__restrict__ off,
+                                          const int *__restrict__ col, const V *__restrict__ val,
+                                          const V *__restrict__ dmat, bool has_d, const T *src,
+                                          const T *nbr, T *dst) {
+  const int o = off[s], wdt = off[s + 1] - o;
+  T a0 = ldv<CG>(src + 3 * row), a1 = ldv<CG>(src + 3 * row + 1), a2 = ldv<CG>(src + 3 * row + 2);
+  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
+  if (has_d) {
+    const V *d = dmat + (size_t)s * 9 * 32 + lane;
+    T dd[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) dd[e] = (T)ldg_stream(d + e * 32);
+    const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
+    const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
+    const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
+    a0 = z0; a1 = z1; a2 = z2;
+  }
+  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+}
+
+// One color of a triangular sweep, one launch per color.
 // L sweep: B = L, src = p, nbr = dst = p^ (colors ascending; ilu0.vhd:413-416);
 // U sweep: B = U, D = Dinv, src = nbr = dst = p^ (colors descending;
 // ilu0.vhd:293-323,407-411). The same kernel runs the transposed sweeps of
 // the adjoint with B = U^T (D = Dinv^T) and B = L^T.
 template <typename V, typename T, bool HAS_D>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__ off,
         const int *__restrict__ col, const V *__restrict__ val, const V *__restrict__ dmat,
         const T *src, const T *nbr, T *dst) {
   if (ctl->done) return;
   const int t = blockIdx.x * kThreads + threadIdx.x;
   if (t >= nrows) return;
-  const int row = row0 + t;
-  const int s = slice0 + (t >> 5), lane = t & 31;
-  const int o = off[s], wdt = off[s + 1] - o;
-  T a0 = src[3 * row], a1 = src[3 * row + 1], a2 = src[3 * row + 2];
-  for (int k = 0; k < wdt; ++k) {
-    const size_t slot = (size_t)(o + k);
-    const int c = ldg_stream(col + slot * 32 + lane);
-    if (c < 0) break;
-    const T y0 = nbr[3 * c], y1 = nbr[3 * c + 1], y2 = nbr[3 * c + 2];
-    const V *v = val + slot * 9 * 32 + lane;
-    a0 = fma(-(T)ldg_stream(v + 0 * 32), y0, a0);
-    a0 = fma(-(T)ldg_stream(v + 1 * 32), y1, a0);
-    a0 = fma(-(T)ldg_stream(v + 2 * 32), y2, a0);
-    a1 = fma(-(T)ldg_stream(v + 3 * 32), y0, a1);
-    a1 = fma(-(T)ldg_stream(v + 4 * 32), y1, a1);
-    a1 = fma(-(T)ldg_stream(v + 5 * 32), y2, a1);
-    a2 = fma(-(T)ldg_stream(v + 6 * 32), y0, a2);
-    a2 = fma(-(T)ldg_stream(v + 7 * 32), y1, a2);
-    a2 = fma(-(T)ldg_stream(v + 8 * 32), y2, a2);
+  sweep_row<V, T, false>(row0 + t, slice0 + (t >> 5), t & 31, off, col, val, dmat, HAS_D, src,
+                         nbr, dst);
+}
+
+// --------------------------------------------------------------------------
+// whole preconditioner apply in one cooperative launch
+// --------------------------------------------------------------------------
+
+// One color step of a sweep: rows [row0, row0+nrows) starting at slice
+// slice0, matrix 0 (L, or U^T in the adjoint; own rows read from src) or
+// matrix 1 (U, or L^T; own rows read from hat), with or without D.
+struct Phase {
+  int row0, nrows, slice0, mat, has_d;
+};
+constexpr int kMaxPhases = 96;
+struct PhaseList {
+  int n;
+  Phase p[kMaxPhases];
+};
+
+// Every spin is bounded: a barrier that does not complete within this many
+// polls marks the run failed (Ctl::bar_fail) and the kernel returns.
+constexpr unsigned int kBarrierSpins = 1u << 22;
+
+// Sense-reversing grid barrier for a cooperative launch (all CTAs resident).
+// The generation is read before arriving; the last CTA to arrive resets the
+// count and bumps the generation. Returns false after a timed-out wait.
+__device__ __forceinline__ bool grid_barrier(Ctl *c) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *gen = &c->bar_gen;
+    const unsigned int g = *gen;
+    ok = 1;
+    __threadfence();
+    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
+      c->bar_count = 0u;
+      __threadfence();
+      atomicAdd(&c->bar_gen, 1u);
+    } else {
+      unsigned int spins = 0;
+      while (*gen == g) {
+        if (++spins > kBarrierSpins) {
+          ok = 0;
+          atomicExch(&c->bar_fail, 1);
+          c->status = ST_TIMEOUT;     // the solve stops: every later kernel
+          __threadfence();            // of the run sees done and returns
+          atomicExch(&c->done, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
   }
-  if (HAS_D) {
-    const V *d = dmat + (size_t)s * 9 * 32 + lane;
-    const T z0 = (T)d[0 * 32] * a0 + (T)d[1 * 32] * a1 + (T)d[2 * 32] * a2;
-    const T z1 = (T)d[3 * 32] * a0 + (T)d[4 * 32] * a1 + (T)d[5 * 32] * a2;
-    const T z2 = (T)d[6 * 32] * a0 + (T)d[7 * 32] * a1 + (T)d[8 * 32] * a2;
-    a0 = z0; a1 = z1; a2 = z2;
+  __syncthreads();
+  return ok != 0;
+}
+
+// hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
+// launch, a grid barrier between consecutive steps. Vector loads go through
+// L2 because earlier steps of the same launch wrote them on other SMs.
+template <typename V, typename T>
+__global__ void __launch_bounds__(kThreads, 2)
+k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__restrict__ col1,
+           const V *__restrict__ val1, const int *__restrict__ off2, const int *__restrict__ col2,
+           const V *__restrict__ val2, const V *__restrict__ dmat, const T *src, T *hat) {
+  if (ctl->done) return;
+  const int stride = gridDim.x * kThreads;
+  for (int q = 0; q < ph.n; ++q) {
+    const Phase P = ph.p[q];
+    const int *off = P.mat ? off2 : off1;
+    const int *col = P.mat ? col2 : col1;
+    const V *val = P.mat ? val2 : val1;
+    const T *own = P.mat ? hat : src;
+    for (int t = blockIdx.x * kThreads + threadIdx.x; t < P.nrows; t += stride)
+      sweep_row<V, T, true>(P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
+                            P.has_d != 0, own, hat, hat);
+    if (q + 1 < ph.n && !grid_barrier(ctl)) return;
   }
-  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
 }
 
 // --------------------------------------------------------------------------
@@ -444,10 +565,15 @@ k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
 // p^ = p on the first color's unknowns. Also drives the graph's while loop.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_update_p(const Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
+k_update_p(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
            T *__restrict__ p, T *__restrict__ ph, unsigned long long cond) {
-  if (cond && blockIdx.x == 0 && threadIdx.x == 0)
-    cudaGraphSetConditional((cudaGraphConditionalHandle)cond, ctl->done ? 0u : 1u);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->body_runs += 1;
+    // hard stop as a second guard: the loop can never run past maxit + 1
+    if (cond)
+      cudaGraphSetConditional((cudaGraphConditionalHandle)cond,
+                              (ctl->done || ctl->body_runs > ctl->maxit + 1) ? 0u : 1u);
+  }
   if (ctl->done) return;
   const T beta = (T)ctl->beta, omega = (T)ctl->omega;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {

@@ -75,6 +75,9 @@ typedef struct {
   int inner_maxit;    /* mixed: iteration limit of each inner solve */
   int max_outer;      /* mixed: refinement step limit */
   int verbose;        /* 0 quiet, 1 INFO lines on stdout */
+  int sweep_mode;     /* 1: the whole ILU0 apply is one cooperative launch
+                         with a grid barrier between colors (default);
+                         0: one launch per color */
 } gbilu_options;
 
 typedef struct {
