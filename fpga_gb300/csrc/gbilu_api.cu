@@ -93,6 +93,7 @@ struct Handle {
   int per_iter[2] = {0, 0};                // launches per iteration [transpose]
   long long last_launches = 0;
   PhaseList phases[2];                     // color steps [transpose]
+  cudaError_t launch_err = cudaSuccess;    // first failed cooperative launch
   int coop_grid64 = 1, coop_grid32 = 1;    // CTAs of the cooperative apply
   size_t device_bytes = 0;
 
@@ -117,6 +118,18 @@ namespace {
       return h->fail(GBILU_CUDA_ERROR, "%s: %s (%s:%d)", #call,                  \
                      cudaGetErrorString(e_), __FILE__, __LINE__);                \
   } while (0)
+
+// the first launch error since the last check (cooperative launches report
+// theirs through their return code)
+cudaError_t last_error(Handle *h) {
+  const cudaError_t e = cudaGetLastError();
+  if (h->launch_err != cudaSuccess) {
+    const cudaError_t le = h->launch_err;
+    h->launch_err = cudaSuccess;
+    return le;
+  }
+  return e;
+}
 
 int grid_for(const Handle *h, long long work) {
   long long g = (work + kThreads - 1) / kThreads;
@@ -195,8 +208,9 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, o.off1, o.col1, o.val1, o.off2,
-                       o.col2, o.val2, o.dmat, src, hat);
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, o.off1, o.col1,
+                                             o.val1, o.off2, o.col2, o.val2, o.dmat, src, hat);
+    if (e != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = e;
     ++launches;
     return;
   }
@@ -338,7 +352,7 @@ int run_loop(Handle *h, bool transpose, int maxit, long long &launches) {
   }
   k_finish_x<T><<<grid_for(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, o.vec->x.p, o.vec->ph.p);
   launches += 1;
-  CK(cudaGetLastError());
+  CK(last_error(h));
   return GBILU_OK;
 }
 
@@ -743,7 +757,7 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   if (!device_ptrs && c.status != ST_ALREADY)
     CK(cudaMemcpyAsync(x, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  CK(cudaGetLastError());
+  CK(last_error(h));
   const int outer = r->outer_iters, inner = r->inner_half_iters;
   const double tr = r->true_relres;
   fill_result(h, c, r);
@@ -791,7 +805,7 @@ int gbilu_apply_spmv(void *handle, const double *x, double *y, int transpose) {
   k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, w.v.p, h->io64b.p);
   CK(cudaMemcpyAsync(y, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  CK(cudaGetLastError());
+  CK(last_error(h));
   h->last_launches = launches + 2;
   return GBILU_OK;
 }
@@ -817,7 +831,7 @@ int gbilu_apply_ilu(void *handle, const double *p, double *z, int transpose) {
   k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, w.ph.p, h->io64b.p);
   CK(cudaMemcpyAsync(z, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  CK(cudaGetLastError());
+  CK(last_error(h));
   h->last_launches = launches + 3;
   return GBILU_OK;
 }
@@ -844,7 +858,7 @@ int gbilu_adjoint(void *handle, const double *g_in, const double *x, double *lam
                                                       h->v64.r.p, h->v64.s.p, h->dA.p);
     CK(cudaMemcpyAsync(dA, h->dA.p, (size_t)h->an.nnzb * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    CK(cudaGetLastError());
+    CK(last_error(h));
   }
   return GBILU_OK;
 }
@@ -935,7 +949,7 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   for (int i = 0; i < reps; ++i) run(launches);
   CK(cudaEventRecord(h->e1, h->st));
   CK(cudaEventSynchronize(h->e1));
-  CK(cudaGetLastError());
+  CK(last_error(h));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->e0, h->e1));
   if (avg_ms) *avg_ms = ms / reps;
