@@ -197,6 +197,20 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
 const char *gbilu_status_string(int status);
 const char *gbilu_last_error(void *handle);
 
+/* Allocation-free y = A x and *d_dot = (y, w) on plain BSR device arrays
+ * (rowptr[nb+1], colind, vals[nnzb*9], x, y, w[3*nb], one double for the
+ * dot), enqueued on `stream` (a cudaStream_t, NULL = default stream). No
+ * counterpart in the reference. For callers that cannot allocate device
+ * memory or create a handle (a fixed device arena, a callback, their own
+ * graph capture): it calls no cudaMalloc/cudaFree; its reduction scratch is
+ * a fixed ~32 KiB device array inside the library, which limits nb to
+ * 1,048,576 block rows (larger nb -> GBILU_BAD_INPUT). The first call on a
+ * device looks that array up and should precede any stream capture; calls
+ * that overlap on the GPU share the array and race. */
+int gbilu_bsr_spmv_dot_noalloc(int nb, const int *d_rowptr, const int *d_colind,
+                               const double *d_vals, const double *d_x, double *d_y,
+                               const double *d_w, double *d_dot, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
