@@ -147,7 +147,8 @@ void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, cons
   const Analysis &an = h->an;
   const int row0 = an.color_ptr[c], nrows = an.color_ptr[c + 1] - row0;
   if (nrows <= 0) return;
-  k_sweep<V, T, D><<<(nrows + kThreads - 1) / kThreads, kThreads, 0, s>>>(
+  const long long threads = nrows <= kSmallRows ? (long long)nrows * kRowLanes : nrows;
+  k_sweep<V, T, D><<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, s>>>(
       h->ctl.p, row0, nrows, an.slice_color_ptr[c], off, col, val, dmat, src, nbr, dst);
   ++launches;
 }
@@ -182,11 +183,13 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
 template <typename V, typename T>
 int coop_grid(Handle *h) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kThreads, 0);
-  int most = 0;
-  for (int c = 0; c < h->an.ncolors; ++c)
-    most = std::max(most, h->an.color_ptr[c + 1] - h->an.color_ptr[c]);
-  const int need = (most + kThreads - 1) / kThreads;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kCoopThreads, 0);
+  long long most = 0;
+  for (int c = 0; c < h->an.ncolors; ++c) {
+    const long long rows = h->an.color_ptr[c + 1] - h->an.color_ptr[c];
+    most = std::max(most, rows <= kSmallRows ? rows * kRowLanes : rows);
+  }
+  const int need = (int)((most + kCoopThreads - 1) / kCoopThreads);
   return std::max(1, std::min(per_sm * h->sm_count, need));
 }
 
@@ -203,7 +206,7 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.gridDim = dim3(sizeof(T) == 8 ? h->coop_grid64 : h->coop_grid32);
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(kCoopThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = attr;
@@ -241,7 +244,10 @@ template <typename V, typename T, int MODE>
 void spmv(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *x, T *y, const T *w,
           int &launches) {
   const int S = h->an.S;
-  k_spmv<V, T, MODE><<<(S + kWarps - 1) / kWarps, kThreads, 0, s>>>(
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv<V, T, MODE>, kThreads, 0);
+  const int grid = std::max(1, std::min((S + kWarps - 1) / kWarps, std::max(1, per_sm) * h->sm_count));
+  k_spmv<V, T, MODE><<<grid, kThreads, 0, s>>>(
       h->ctl.p, S, h->srows.p, o.offA, o.colA, o.valA, x, y, w, h->partials.p);
   ++launches;
 }

@@ -273,11 +273,13 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
        T *__restrict__ y, const T *__restrict__ w, double *partials) {
   if (MODE != SPMV_PLAIN && MODE != SPMV_RESID && ctl->done) return;
-  const int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  // persistent grid: each warp walks slices warp, warp + all warps, ...;
+  // one reduction per CTA at the end instead of one per 8 slices
   const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * kWarps;
   double d1 = 0.0, d2 = 0.0;
   DF f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
-  if (s < S) {
+  for (int s = blockIdx.x * kWarps + (threadIdx.x >> 5); s < S; s += nwarps) {
     const int2 sr = srows[s];
     if (lane < sr.y) {
       const int row = sr.x + lane;
@@ -289,13 +291,13 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
       }
       y[3 * row] = a0; y[3 * row + 1] = a1; y[3 * row + 2] = a2;
       if (MODE == SPMV_RESID) {
-        if (sizeof(T) == 8) d1 = (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
+        if (sizeof(T) == 8) d1 += (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
         else { df_add_prod(f1, (float)a0, (float)a0); df_add_prod(f1, (float)a1, (float)a1); df_add_prod(f1, (float)a2, (float)a2); }
       } else if (MODE == SPMV_ALPHA || MODE == SPMV_OMEGA) {
         const T w0 = w[3 * row], w1 = w[3 * row + 1], w2 = w[3 * row + 2];
         if (sizeof(T) == 8) {
-          d1 = (double)a0 * w0 + (double)a1 * w1 + (double)a2 * w2;
-          if (MODE == SPMV_OMEGA) d2 = (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
+          d1 += (double)a0 * w0 + (double)a1 * w1 + (double)a2 * w2;
+          if (MODE == SPMV_OMEGA) d2 += (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
         } else {
           df_add_prod(f1, (float)a0, (float)w0); df_add_prod(f1, (float)a1, (float)w1); df_add_prod(f1, (float)a2, (float)w2);
           if (MODE == SPMV_OMEGA) { df_add_prod(f2, (float)a0, (float)a0); df_add_prod(f2, (float)a1, (float)a1); df_add_prod(f2, (float)a2, (float)a2); }
@@ -334,7 +336,21 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
 // one color of a triangular sweep
 // --------------------------------------------------------------------------
 
-// One row of a sweep: dst_i = [D_i] (src_i - sum_j B_ij nbr_j).
+// D multiply of one row: (a0, a1, a2) <- D_s,lane (a0, a1, a2)
+template <typename V, typename T>
+__device__ __forceinline__ void apply_d(const V *__restrict__ dmat, int s, int lane, T &a0, T &a1,
+                                        T &a2) {
+  const V *d = dmat + (size_t)s * 9 * 32 + lane;
+  T dd[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) dd[e] = (T)ldg_stream(d + e * 32);
+  const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
+  const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
+  const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
+  a0 = z0; a1 = z1; a2 = z2;
+}
+
+// One row of a sweep, one thread: dst_i = [D_i] (src_i - sum_j B_ij nbr_j).
 template <typename V, typename T, bool CG>
 __device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *__restrict__ off,
                                           const int *__restrict__ col, const V *__restrict__ val,
@@ -343,24 +359,61 @@ __device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *_
   const int o = off[s], wdt = off[s + 1] - o;
   T a0 = ldv<CG>(src + 3 * row), a1 = ldv<CG>(src + 3 * row + 1), a2 = ldv<CG>(src + 3 * row + 2);
   row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
-  if (has_d) {
-    const V *d = dmat + (size_t)s * 9 * 32 + lane;
-    T dd[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) dd[e] = (T)ldg_stream(d + e * 32);
-    const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
-    const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
-    const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
-    a0 = z0; a1 = z1; a2 = z2;
-  }
+  if (has_d) apply_d(dmat, s, lane, a0, a1, a2);
   dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+}
+
+// Colors with at most kSmallRows rows are latency-bound (a few thousand rows
+// cannot fill the GPU), so they use 8 lanes per row: lane j of the group
+// takes blocks j, j+8, ... (one memory round trip for the column, one for
+// the gather and the values), then the partial sums meet in xor shuffles.
+constexpr int kSmallRows = 16384;
+constexpr int kRowLanes = 8;
+
+// All 32 lanes of a warp call this together (rows past the end pass
+// valid = false); group g = t / 8 owns row row0 + g.
+template <typename V, typename T, bool CG>
+__device__ __forceinline__ void sweep_row8(bool valid, int row, int s, int lane, int j,
+                                           const int *__restrict__ off, const int *__restrict__ col,
+                                           const V *__restrict__ val, const V *__restrict__ dmat,
+                                           bool has_d, const T *src, const T *nbr, T *dst) {
+  T a0 = 0, a1 = 0, a2 = 0;
+  if (valid) {
+    const int o = off[s], wdt = off[s + 1] - o;
+    for (int k = j; k < wdt; k += kRowLanes) {
+      const int c = ldg_stream(col + (size_t)(o + k) * 32 + lane);
+      if (c < 0) break;
+      const V *v = val + (size_t)(o + k) * 9 * 32 + lane;
+      V bv[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) bv[e] = ldg_stream(v + e * 32);
+      const T y0 = ldv<CG>(nbr + 3 * c), y1 = ldv<CG>(nbr + 3 * c + 1), y2 = ldv<CG>(nbr + 3 * c + 2);
+      a0 = fma(-(T)bv[0], y0, a0); a0 = fma(-(T)bv[1], y1, a0); a0 = fma(-(T)bv[2], y2, a0);
+      a1 = fma(-(T)bv[3], y0, a1); a1 = fma(-(T)bv[4], y1, a1); a1 = fma(-(T)bv[5], y2, a1);
+      a2 = fma(-(T)bv[6], y0, a2); a2 = fma(-(T)bv[7], y1, a2); a2 = fma(-(T)bv[8], y2, a2);
+    }
+  }
+#pragma unroll
+  for (int m = kRowLanes / 2; m > 0; m >>= 1) {
+    a0 += __shfl_xor_sync(0xffffffffu, a0, m);
+    a1 += __shfl_xor_sync(0xffffffffu, a1, m);
+    a2 += __shfl_xor_sync(0xffffffffu, a2, m);
+  }
+  if (valid && j == 0) {
+    a0 += ldv<CG>(src + 3 * row);
+    a1 += ldv<CG>(src + 3 * row + 1);
+    a2 += ldv<CG>(src + 3 * row + 2);
+    if (has_d) apply_d(dmat, s, lane, a0, a1, a2);
+    dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+  }
 }
 
 // One color of a triangular sweep, one launch per color.
 // L sweep: B = L, src = p, nbr = dst = p^ (colors ascending; ilu0.vhd:413-416);
 // U sweep: B = U, D = Dinv, src = nbr = dst = p^ (colors descending;
 // ilu0.vhd:293-323,407-411). The same kernel runs the transposed sweeps of
-// the adjoint with B = U^T (D = Dinv^T) and B = L^T.
+// the adjoint with B = U^T (D = Dinv^T) and B = L^T. Small colors
+// (nrows <= kSmallRows) are launched with 8 threads per row.
 template <typename V, typename T, bool HAS_D>
 __global__ void __launch_bounds__(kThreads, 2)
 k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__ off,
@@ -368,6 +421,13 @@ k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__
         const T *src, const T *nbr, T *dst) {
   if (ctl->done) return;
   const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (nrows <= kSmallRows) {
+    const int g = t / kRowLanes;
+    if ((t & ~31) / kRowLanes >= nrows) return;   // the whole warp is past the end
+    sweep_row8<V, T, false>(g < nrows, row0 + g, slice0 + (g >> 5), g & 31, t % kRowLanes, off,
+                            col, val, dmat, HAS_D, src, nbr, dst);
+    return;
+  }
   if (t >= nrows) return;
   sweep_row<V, T, false>(row0 + t, slice0 + (t >> 5), t & 31, off, col, val, dmat, HAS_D, src,
                          nbr, dst);
@@ -388,6 +448,8 @@ struct PhaseList {
   int n;
   Phase p[kMaxPhases];
 };
+
+constexpr int kCoopThreads = 512;     // one CTA per SM: half the barrier arrivals
 
 // Every spin is bounded: a barrier that does not complete within this many
 // polls marks the run failed (Ctl::bar_fail) and the kernel returns.
@@ -419,7 +481,7 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c) {
           atomicExch(&c->done, 1);
           break;
         }
-        __nanosleep(32);
+        if (spins > 64) __nanosleep(32);
       }
     }
     __threadfence();
@@ -432,21 +494,30 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c) {
 // launch, a grid barrier between consecutive steps. Vector loads go through
 // L2 because earlier steps of the same launch wrote them on other SMs.
 template <typename V, typename T>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kCoopThreads, 1)
 k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__restrict__ col1,
            const V *__restrict__ val1, const int *__restrict__ off2, const int *__restrict__ col2,
            const V *__restrict__ val2, const V *__restrict__ dmat, const T *src, T *hat) {
   if (ctl->done) return;
-  const int stride = gridDim.x * kThreads;
+  const int stride = gridDim.x * kCoopThreads;
   for (int q = 0; q < ph.n; ++q) {
     const Phase P = ph.p[q];
     const int *off = P.mat ? off2 : off1;
     const int *col = P.mat ? col2 : col1;
     const V *val = P.mat ? val2 : val1;
     const T *own = P.mat ? hat : src;
-    for (int t = blockIdx.x * kThreads + threadIdx.x; t < P.nrows; t += stride)
-      sweep_row<V, T, true>(P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
-                            P.has_d != 0, own, hat, hat);
+    if (P.nrows <= kSmallRows) {
+      const int span = ((P.nrows * kRowLanes + 31) / 32) * 32;   // whole warps
+      for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < span; t += stride) {
+        const int g = t / kRowLanes;
+        sweep_row8<V, T, true>(g < P.nrows, P.row0 + g, P.slice0 + (g >> 5), g & 31,
+                               t % kRowLanes, off, col, val, dmat, P.has_d != 0, own, hat, hat);
+      }
+    } else {
+      for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < P.nrows; t += stride)
+        sweep_row<V, T, true>(P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
+                              P.has_d != 0, own, hat, hat);
+    }
     if (q + 1 < ph.n && !grid_barrier(ctl)) return;
   }
 }
