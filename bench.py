@@ -219,6 +219,7 @@ def gpu_bench(args, world, rank, local):
     for name in ("spmv64", "ilu64", "spmv32", "ilu32"):
         ms, by, la = g.bench_kernel(name, reps=20)
         kern[name] = {"ms": ms, "alg_bytes": by, "launches": la, "gbs": by / ms / 1e6}
+    trace = {"fp64": g.ilu_trace(fp32=False), "fp32": g.ilu_trace(fp32=True)}
     it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
     solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
     traffic = None
@@ -259,6 +260,7 @@ def gpu_bench(args, world, rank, local):
                "solve_gbs": solve_gbs,
                "solve_frac_of_peak": solve_gbs / peak if solve_gbs else None,
                "kernels": kern,
+               "ilu_phases_rows_us": trace,
                "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": 2 * n * 8,
                        "d2h_bytes_per_step": n * 8},
                "gpu_launches": int(launches),

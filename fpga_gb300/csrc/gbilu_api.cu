@@ -157,6 +157,7 @@ void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, cons
 PhaseList make_phases(const Analysis &an, bool transpose) {
   PhaseList pl;
   pl.n = 0;
+  pl.trace = 0;
   const int C = an.ncolors;
   auto add = [&](int c, int mat, int has_d) {
     Phase &p = pl.p[pl.n++];
@@ -900,6 +901,57 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
     // and the dot operands of the two SpMV epilogues (rt, s)
     const double vec = (17.0 * n + 2.0 * n0) * sx;
     s->alg_bytes_iter[p] = 2 * s->alg_bytes_spmv[p] + 2 * s->alg_bytes_ilu[p] + vec;
+  }
+  return GBILU_OK;
+}
+
+int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows, int cap,
+                    int *nphases) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  if (fp32 && !h->with_32) return h->fail(GBILU_BAD_INPUT, "FP32 trace needs GBILU_MIXED");
+  if (h->an.ncolors > kMaxPhases / 2) return h->fail(GBILU_BAD_INPUT, "too many colors to trace");
+  CK(cudaSetDevice(h->opt.device));
+  const int t = transpose ? 1 : 0;
+  PhaseList pl = h->phases[t];
+  pl.trace = 1;
+  const int n = 3 * h->an.nb;
+  CK(cudaMemsetAsync(h->v64.p.p, 0, n * sizeof(double), h->st));
+  if (h->with_32) CK(cudaMemsetAsync(h->v32.p.p, 0, n * sizeof(float), h->st));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.blockDim = dim3(kCoopThreads);
+  cfg.stream = h->st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  for (int rep = 0; rep < 2; ++rep) {   // the second, warm run is reported
+    k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
+    if (fp32) {
+      Ops<float, float> o = make_ops<float, float>(h, t != 0);
+      cfg.gridDim = dim3(h->coop_grid32);
+      CK(cudaMemsetAsync(h->v32.ph.p, 0, n * sizeof(float), h->st));
+      CK(cudaLaunchKernelEx(&cfg, k_ilu_coop<float, float>, h->ctl.p, pl, o.off1, o.col1, o.val1,
+                            o.off2, o.col2, o.val2, o.dmat, (const float *)h->v32.p.p, h->v32.ph.p));
+    } else {
+      Ops<double, double> o = make_ops<double, double>(h, t != 0);
+      cfg.gridDim = dim3(h->coop_grid64);
+      CK(cudaMemsetAsync(h->v64.ph.p, 0, n * sizeof(double), h->st));
+      CK(cudaLaunchKernelEx(&cfg, k_ilu_coop<double, double>, h->ctl.p, pl, o.off1, o.col1,
+                            o.val1, o.off2, o.col2, o.val2, o.dmat, (const double *)h->v64.p.p,
+                            h->v64.ph.p));
+    }
+  }
+  CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(last_error(h));
+  if (nphases) *nphases = pl.n;
+  for (int q = 0; q < pl.n && q < cap; ++q) {
+    if (us) us[q] = (h->h_ctl->phase_ns[q + 1] - h->h_ctl->phase_ns[q]) * 1e-3;
+    if (rows) rows[q] = pl.p[q].nrows;
   }
   return GBILU_OK;
 }

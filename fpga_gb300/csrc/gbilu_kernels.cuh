@@ -27,6 +27,8 @@ enum Status {
   ST_TIMEOUT = 5
 };
 
+constexpr int kMaxPhases = 96;                // color steps of one ILU apply
+
 // Device-resident solver state, one per solve in flight.
 struct Ctl {
   double rho, alpha, omega, beta;
@@ -43,6 +45,7 @@ struct Ctl {
   unsigned int bar_count, bar_gen;  // grid barrier of cooperative launches
   int bar_fail;                   // a barrier wait timed out
   int body_runs;                  // loop bodies run (graph launches count)
+  unsigned long long phase_ns[kMaxPhases + 1];   // traced ILU apply: phase starts
 };
 
 // --------------------------------------------------------------------------
@@ -443,9 +446,9 @@ k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__
 struct Phase {
   int row0, nrows, slice0, mat, has_d;
 };
-constexpr int kMaxPhases = 96;
 struct PhaseList {
   int n;
+  int trace;                      // CTA 0 stamps %globaltimer at each phase start
   Phase p[kMaxPhases];
 };
 
@@ -501,6 +504,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__re
   if (ctl->done) return;
   const int stride = gridDim.x * kCoopThreads;
   for (int q = 0; q < ph.n; ++q) {
+    if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
     const Phase P = ph.p[q];
     const int *off = P.mat ? off2 : off1;
     const int *col = P.mat ? col2 : col1;
@@ -519,6 +523,11 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__re
                               P.has_d != 0, own, hat, hat);
     }
     if (q + 1 < ph.n && !grid_barrier(ctl)) return;
+    if (ph.trace && q + 1 == ph.n) {
+      // the end of the last phase: after every CTA finished it
+      if (!grid_barrier(ctl)) return;
+      if (blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[ph.n] = globaltimer();
+    }
   }
 }
 

@@ -102,6 +102,7 @@ def load():
     L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
     L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    L.gbilu_ilu_trace.argtypes = [VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_int)]
     L.gbilu_status_string.argtypes = [C.c_int]
     L.gbilu_status_string.restype = C.c_char_p
     L.gbilu_last_error.argtypes = [VP]
@@ -245,6 +246,15 @@ class GbIlu:
         return s.as_dict()
 
     KERNELS = {"spmv64": 0, "ilu64": 1, "spmv32": 2, "ilu32": 3}
+
+    def ilu_trace(self, fp32=False, transpose=False):
+        """[(rows, microseconds)] per color step of one single-launch ILU apply."""
+        us = np.zeros(96)
+        rows = np.zeros(96, np.int32)
+        n = C.c_int()
+        self._check(self.L.gbilu_ilu_trace(self.h, int(fp32), int(transpose), us.ctypes.data,
+                                           rows.ctypes.data, 96, C.byref(n)))
+        return [(int(rows[i]), float(us[i])) for i in range(n.value)]
 
     def bench_kernel(self, which, reps=20):
         """(avg ms, algorithmic bytes, launches) per application of a kernel family."""

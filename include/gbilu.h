@@ -194,6 +194,15 @@ int gbilu_get_stats(void *handle, gbilu_stats *stats);
 int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
                        double *alg_bytes, int *launches);
 
+/* Traced ILU apply: runs the single-launch preconditioner apply (FP64, or
+ * FP32 with GBILU_MIXED; forward or transposed) with device timestamps at
+ * every color step and returns each step's duration in microseconds (the
+ * step plus the grid barrier after it) and its row count. The GB300
+ * counterpart of the reference's periodic debug lines (solver.vhd:1106-1133),
+ * per color step instead of per sampling interval. */
+int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows,
+                    int cap, int *nphases);
+
 const char *gbilu_status_string(int status);
 const char *gbilu_last_error(void *handle);
 

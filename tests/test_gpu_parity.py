@@ -99,6 +99,15 @@ def test_sweep_modes_bit_identical(case):
     assert r1.half_iters == r2.half_iters and np.array_equal(x1, x2)
 
 
+def test_ilu_trace(case):
+    s, P, g = case
+    for transpose in (False, True):
+        tr = g.ilu_trace(transpose=transpose)
+        C = P.ncolors
+        assert len(tr) == (max(1, 2 * C - 2) if not transpose else 2 * C - 1)
+        assert sum(r for r, _ in tr) >= s.nb and all(us >= 0 for _, us in tr)
+
+
 def test_deterministic(case):
     s, P, g = case
     x1, _ = g.solve(s.b, tol=1e-6, maxit=500)
