@@ -210,7 +210,10 @@ __device__ __forceinline__ void finish_init(Ctl *c, double rr) {
 // one sliced row: a += sign * sum_k B_k x_{c_k}
 // --------------------------------------------------------------------------
 
-constexpr int kBatch = 4;   // blocks whose loads are in flight together
+#ifndef GBILU_BATCH
+#define GBILU_BATCH 4
+#endif
+constexpr int kBatch = GBILU_BATCH;   // blocks whose loads are in flight together
 
 // Loads of vectors that other CTAs of the same kernel wrote go through L2
 // (ld.global.cg): the per-SM L1 is not coherent inside one launch.
@@ -361,8 +364,26 @@ __device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *_
                                           const T *nbr, T *dst) {
   const int o = off[s], wdt = off[s + 1] - o;
   T a0 = ldv<CG>(src + 3 * row), a1 = ldv<CG>(src + 3 * row + 1), a2 = ldv<CG>(src + 3 * row + 2);
+#if GBILU_EARLY_D
+  // the inverse diagonal block does not depend on the row's columns: load it
+  // before the column chain so that it arrives with the first batch
+  V dd[9];
+  if (has_d) {
+    const V *d = dmat + (size_t)s * 9 * 32 + lane;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) dd[e] = ldg_stream(d + e * 32);
+  }
+  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
+  if (has_d) {
+    const T z0 = (T)dd[0] * a0 + (T)dd[1] * a1 + (T)dd[2] * a2;
+    const T z1 = (T)dd[3] * a0 + (T)dd[4] * a1 + (T)dd[5] * a2;
+    const T z2 = (T)dd[6] * a0 + (T)dd[7] * a1 + (T)dd[8] * a2;
+    a0 = z0; a1 = z1; a2 = z2;
+  }
+#else
   row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
   if (has_d) apply_d(dmat, s, lane, a0, a1, a2);
+#endif
   dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
 }
 
@@ -370,6 +391,9 @@ __device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *_
 // cannot fill the GPU), so they use 8 lanes per row: lane j of the group
 // takes blocks j, j+8, ... (one memory round trip for the column, one for
 // the gather and the values), then the partial sums meet in xor shuffles.
+#ifndef GBILU_EARLY_D
+#define GBILU_EARLY_D 0
+#endif
 constexpr int kSmallRows = 16384;
 constexpr int kRowLanes = 8;
 
@@ -452,7 +476,10 @@ struct PhaseList {
   Phase p[kMaxPhases];
 };
 
-constexpr int kCoopThreads = 512;     // one CTA per SM: half the barrier arrivals
+#ifndef GBILU_COOP_THREADS
+#define GBILU_COOP_THREADS 512
+#endif
+constexpr int kCoopThreads = GBILU_COOP_THREADS;   // one CTA per SM: half the barrier arrivals
 
 // Every spin is bounded: a barrier that does not complete within this many
 // polls marks the run failed (Ctl::bar_fail) and the kernel returns.
