@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libgbilu.so")
-SOURCES = ["gbilu_host.cpp", "gbilu_api.cu", "gbilu_noalloc.cu"]
+SOURCES = ["gbilu_host.cpp", "gbilu_api.cu", "gbilu_noalloc.cu", "gbilu_fpga_compat.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -12,6 +12,7 @@ int color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
   // First-fit greedy in natural order: a row takes the smallest color that no
   // already colored neighbour holds. stamp[c] == i+1 marks color c as taken
   // for row i.
+  if (nb <= 0) return 0;
   std::vector<int> stamp(static_cast<size_t>(nb) + 1, 0);
   int ncolors = 0;
   std::fill(color, color + nb, -1);

@@ -206,6 +206,42 @@ int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows
 const char *gbilu_status_string(int status);
 const char *gbilu_last_error(void *handle);
 
+/* --- interchange with the Alveo kernel's host-side formats (host only) --- */
+
+/* Bank layout of the five data buffers and the 40-word (5-cacheline) setup
+ * array, as fpga_setup_host_datamem builds them
+ * (fpga_functions_bicgstab.cpp:84-496, port configuration 2r_3r3w).
+ * processed_sizes[18] as there (row, val, colors, columns, new-row, block-diag
+ * sizes of A, then of L, then of U), nnz_sizes[3] = value counts of A, L, U.
+ * Outputs: setup[40], totals[5] (bytes per bank), offsets[23] (byte offset of
+ * setup, nnz, L/U nnz, color sizes, L/U color sizes, block diag | P indices,
+ * L/U P indices, col indices, L/U col indices, NRs, L/U NRs | X2, R1 | X1, R2
+ * | L res, U res inside their bank; may be NULL) and result_offsets[6] (X
+ * even, R even, X odd, R odd, L res, U res; may be NULL). debug_bytes must be
+ * a whole number of 64-byte lines, else GBILU_BAD_INPUT. */
+int gbilu_fpga_layout(unsigned int config_bits, const int *processed_sizes,
+                      const int *nnz_sizes, unsigned int debug_bytes,
+                      unsigned long long *setup, unsigned int *totals,
+                      long long *offsets, unsigned int *result_offsets);
+
+/* Packs the backend's vectorPointers (indices as in
+ * fpga_functions_bicgstab.cpp:606-629) into the five banks exactly as
+ * fpga_copy_host_datamem does after a reset: setup array first, color sizes
+ * past their 8-int header, results sentinels in the padding of X2/R2 when
+ * fill_results is set. banks[b] must hold totals[b] bytes of
+ * gbilu_fpga_layout. */
+int gbilu_fpga_pack(unsigned int config_bits, const int *processed_sizes,
+                    const int *nnz_sizes, void *const *vector_pointers,
+                    const int *vector_sizes, int fill_results,
+                    unsigned char *const *banks);
+
+/* Writes a solve's outcome as the kernel's debug buffer (lines x 8 words):
+ * line 0 = general status (signature, aborted / no-results flags, run length
+ * in ns), line 1 = final status line (half-iteration counter, four-norm ring),
+ * the rest the "unwritten" marker, so decode_debuginfo_bicgstab
+ * (bicgstab_utils.cpp:90-280) reads GB300 runs. lines >= 2. */
+int gbilu_status_lines(const gbilu_result *res, unsigned long long *buf, int lines);
+
 /* Allocation-free y = A x and *d_dot = (y, w) on plain BSR device arrays
  * (rowptr[nb+1], colind, vals[nnzb*9], x, y, w[3*nb], one double for the
  * dot), enqueued on `stream` (a cudaStream_t, NULL = default stream). No
