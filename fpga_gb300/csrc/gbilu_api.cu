@@ -34,9 +34,12 @@ template <typename T> struct DevBuf {
 // device copy of one sliced matrix
 struct DevMat {
   DevBuf<int> off, col;
+  DevBuf<int> vsrc;          // source block per slot lane (device factorization)
+  bool transpose = false;
+  long long slots = 0;
   DevBuf<double> v64;
   DevBuf<float> v32;
-  void release() { off.release(); col.release(); v64.release(); v32.release(); }
+  void release() { off.release(); col.release(); vsrc.release(); v64.release(); v32.release(); }
 };
 
 // the nine work vectors of one BiCGSTAB run
@@ -86,6 +89,10 @@ struct Handle {
   Vecs<double> v64;
   Vecs<float> v32;
   DevBuf<double> b64, io64, io64b, partials, dA;
+  // device factorization: permuted values (factored in place), inverses
+  DevBuf<int> pdiag, bad;
+  DevBuf<double> pbuf, vals_in, dinvp;
+  bool host_factors_stale = false;
   DevBuf<Ctl> ctl;                         // [0] main run, [1] refinement residual
   Ctl *h_ctl = nullptr;                    // pinned mirror
   bool with_t = false, with_32 = false;
@@ -385,8 +392,15 @@ int upload_mat(Handle *h, const SlicedMatrix &m, DevMat &d) {
   CK(cudaMemcpy(d.off.p, m.off.data(), m.off.size() * sizeof(int), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(d.col.p, m.col.data(), m.col.size() * sizeof(int), cudaMemcpyHostToDevice));
   const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
+  d.slots = m.slots();
+  d.transpose = m.transpose_blocks;
   CK(d.v64.alloc(nv));
   if (h->with_32) CK(d.v32.alloc(nv));
+  if (h->opt.factor_on_device) {
+    CK(d.vsrc.alloc(m.vsrc.size()));
+    CK(cudaMemcpy(d.vsrc.p, m.vsrc.data(), m.vsrc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    h->device_bytes += m.vsrc.size() * sizeof(int);
+  }
   h->device_bytes += (m.off.size() + m.col.size()) * sizeof(int) + nv * 8 + (h->with_32 ? nv * 4 : 0);
   return GBILU_OK;
 }
@@ -424,6 +438,8 @@ void release_device(Handle *h) {
     for (auto &g : row)
       if (g) { cudaGraphExecDestroy(g); g = nullptr; }
   for (DevMat *m : {&h->A, &h->L, &h->U, &h->At, &h->Ut, &h->Lt}) m->release();
+  h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
+  h->dinvp.release();
   h->srows.release(); h->perm.release(); h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
@@ -480,12 +496,73 @@ int setup_device(Handle *h) {
   const size_t maxgrid = std::max<size_t>((size_t)h->sm_count * 8, (size_t)(an.S + kWarps - 1) / kWarps) + 1;
   CK(h->partials.alloc(2 * maxgrid));
   CK(h->ctl.alloc(2));
+  if (h->opt.factor_on_device) {
+    CK(h->pdiag.alloc(an.nb));
+    CK(cudaMemcpy(h->pdiag.p, an.pdiag.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+    CK(h->bad.alloc(1));
+    CK(h->pbuf.alloc((size_t)an.nnzb * 9));
+    CK(h->vals_in.alloc((size_t)an.nnzb * 9));
+    CK(h->dinvp.alloc((size_t)an.nb * 9));
+    h->device_bytes += (size_t)an.nnzb * 9 * 16 + (size_t)an.nb * 76;
+  }
   h->phases[0] = make_phases(an, false);
   h->phases[1] = make_phases(an, true);
   h->coop_grid64 = coop_grid<double, double>(h);
   h->coop_grid32 = coop_grid<float, float>(h);
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
                      (size_t)an.nnzb * 8 + (size_t)an.nb * 8;
+  return GBILU_OK;
+}
+
+// Sliced values of one matrix (FP64 and, in the mixed mode, FP32) from
+// per-block device values.
+void fill_mat_device(Handle *h, DevMat &m, const double *src) {
+  const int g = grid_for(h, m.slots * 32);
+  k_fill_sliced<double><<<g, kThreads, 0, h->st>>>(m.slots, m.vsrc.p, m.transpose ? 1 : 0, src, m.v64.p);
+  if (h->with_32)
+    k_fill_sliced<float><<<g, kThreads, 0, h->st>>>(m.slots, m.vsrc.p, m.transpose ? 1 : 0, src, m.v32.p);
+}
+
+// Permute, factor and lay out on the device: values in input order (host
+// array) -> color-permuted blocks -> A and A^T slices -> IKJ block ILU(0)
+// color by color in place -> L, U, U^T, L^T and the inverse diagonal blocks.
+int factor_device(Handle *h, const double *vals) {
+  const Analysis &an = h->an;
+  const size_t n9 = (size_t)an.nnzb * 9;
+  CK(cudaMemcpyAsync(h->vals_in.p, vals, n9 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  k_permute_blocks<<<grid_for(h, (long long)n9), kThreads, 0, h->st>>>(an.nnzb, h->psrc.p,
+                                                                       h->vals_in.p, h->pbuf.p);
+  fill_mat_device(h, h->A, h->pbuf.p);
+  fill_mat_device(h, h->At, h->pbuf.p);
+  const int big = 0x7fffffff;
+  CK(cudaMemcpyAsync(h->bad.p, &big, sizeof(int), cudaMemcpyHostToDevice, h->st));
+  for (int c = 0; c < an.ncolors; ++c) {
+    const int row0 = an.color_ptr[c], rows = an.color_ptr[c + 1] - row0;
+    k_bilu0_color<<<(rows + kThreads - 1) / kThreads, kThreads, 0, h->st>>>(
+        row0, rows, h->prowptr.p, h->pcol.p, h->pdiag.p, h->pbuf.p, h->dinvp.p, h->bad.p);
+  }
+  int bad = big;
+  CK(cudaMemcpyAsync(&bad, h->bad.p, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(last_error(h));
+  if (bad != big)
+    return h->fail(GBILU_SINGULAR,
+                   "gbilu_factor: singular diagonal block in permuted row %d (input row %d)", bad,
+                   an.perm[bad]);
+  fill_mat_device(h, h->L, h->pbuf.p);
+  fill_mat_device(h, h->U, h->pbuf.p);
+  fill_mat_device(h, h->Lt, h->pbuf.p);
+  fill_mat_device(h, h->Ut, h->pbuf.p);
+  const int gd = grid_for(h, (long long)an.S * 32);
+  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 0, h->dinvp.p, h->dinv64.p);
+  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 1, h->dinvp.p, h->dinvT64.p);
+  if (h->with_32) {
+    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 0, h->dinvp.p, h->dinv32.p);
+    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 1, h->dinvp.p, h->dinvT32.p);
+  }
+  CK(cudaStreamSynchronize(h->st));
+  CK(last_error(h));
+  h->host_factors_stale = true;
   return GBILU_OK;
 }
 
@@ -687,6 +764,16 @@ int gbilu_factor(void *handle, const double *vals) {
   auto t0 = std::chrono::steady_clock::now();
   h->factored = false;
   const Analysis &an = h->an;
+  if (h->opt.factor_on_device && h->opt.device >= 0) {
+    CK(cudaSetDevice(h->opt.device));
+    const int rc = factor_device(h, vals);
+    if (rc) return rc;
+    h->factored = true;
+    h->factor_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return GBILU_OK;
+  }
+  h->host_factors_stale = false;
   h->pvals.resize((size_t)an.nnzb * 9);
   permute_values(an, vals, h->pvals.data());
   h->lu = h->pvals;
@@ -716,6 +803,15 @@ int gbilu_get_factors(void *handle, double *lu, double *dinv) {
   Handle *h = static_cast<Handle *>(handle);
   if (!h) return GBILU_BAD_INPUT;
   if (!h->factored) return h->fail(GBILU_NOT_READY, "gbilu_factor has not been called");
+  if (h->host_factors_stale) {      // factored on the device: fetch the copies
+    CK(cudaSetDevice(h->opt.device));
+    h->lu.resize((size_t)h->an.nnzb * 9);
+    h->dinv.resize((size_t)h->an.nb * 9);
+    CK(cudaMemcpy(h->lu.data(), h->pbuf.p, h->lu.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(h->dinv.data(), h->dinvp.p, h->dinv.size() * sizeof(double),
+                  cudaMemcpyDeviceToHost));
+    h->host_factors_stale = false;
+  }
   if (lu) memcpy(lu, h->lu.data(), h->lu.size() * sizeof(double));
   if (dinv) memcpy(dinv, h->dinv.data(), h->dinv.size() * sizeof(double));
   return GBILU_OK;

@@ -767,4 +767,136 @@ __global__ void k_grad_a(int nb, const int *__restrict__ prowptr, const int *__r
   }
 }
 
+// --------------------------------------------------------------------------
+// block ILU(0) on the device
+// --------------------------------------------------------------------------
+
+// Every product and sum below is an explicitly rounded IEEE operation in the
+// same order as the host factorization (gbilu_host.cpp), with no fused
+// multiply-add, so the device factors equal the host ones bit for bit.
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+__device__ __forceinline__ void mul3_exact(const double *a, const double *b, double *o) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      o[r * 3 + c] = dadd(dadd(dmul(a[r * 3], b[c]), dmul(a[r * 3 + 1], b[3 + c])),
+                          dmul(a[r * 3 + 2], b[6 + c]));
+}
+
+// 3x3 inverse by cofactors; false when the block is singular or not finite
+__device__ __forceinline__ bool inv3_exact(const double *a, double *o) {
+  const double c00 = dsub(dmul(a[4], a[8]), dmul(a[5], a[7]));
+  const double c01 = dsub(dmul(a[5], a[6]), dmul(a[3], a[8]));
+  const double c02 = dsub(dmul(a[3], a[7]), dmul(a[4], a[6]));
+  const double det = dadd(dadd(dmul(a[0], c00), dmul(a[1], c01)), dmul(a[2], c02));
+  if (det == 0.0 || !isfinite(det)) return false;
+  const double id = __ddiv_rn(1.0, det);
+  o[0] = dmul(c00, id);
+  o[1] = dmul(dsub(dmul(a[2], a[7]), dmul(a[1], a[8])), id);
+  o[2] = dmul(dsub(dmul(a[1], a[5]), dmul(a[2], a[4])), id);
+  o[3] = dmul(c01, id);
+  o[4] = dmul(dsub(dmul(a[0], a[8]), dmul(a[2], a[6])), id);
+  o[5] = dmul(dsub(dmul(a[2], a[3]), dmul(a[0], a[5])), id);
+  o[6] = dmul(c02, id);
+  o[7] = dmul(dsub(dmul(a[1], a[6]), dmul(a[0], a[7])), id);
+  o[8] = dmul(dsub(dmul(a[0], a[4]), dmul(a[1], a[3])), id);
+  return true;
+}
+
+// pv[k] = vals[src[k]] (input order -> color-permuted order), 9 per block
+__global__ void k_permute_blocks(int nnzb, const int *__restrict__ src,
+                                 const double *__restrict__ vals, double *__restrict__ pv) {
+  for (long long i = blockIdx.x * (long long)kThreads + threadIdx.x; i < 9LL * nnzb;
+       i += (long long)gridDim.x * kThreads) {
+    const long long k = i / 9, e = i - 9 * k;
+    pv[i] = vals[(long long)src[k] * 9 + e];
+  }
+}
+
+// IKJ block ILU(0) of the rows of one color (rows of one color are never
+// coupled, and all earlier colors are final): for each k < i in row i,
+// L_ik = A_ik U_kk^-1, then A_ij -= L_ik U_kj for the j > k present in both
+// rows (a merge of the two sorted column lists); D_i^-1 = inv(A_ii).
+// A singular pivot records the smallest failing row in *bad.
+__global__ void k_bilu0_color(int row0, int nrows, const int *__restrict__ rp,
+                              const int *__restrict__ ci, const int *__restrict__ diag,
+                              double *v, double *dinv, int *bad) {
+  const int t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= nrows) return;
+  const int i = row0 + t;
+  const int end = rp[i + 1];
+  for (int kk = rp[i]; kk < diag[i]; ++kk) {
+    const int k = ci[kk];
+    double a[9], dk[9], l[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) { a[e] = v[(size_t)kk * 9 + e]; dk[e] = dinv[(size_t)k * 9 + e]; }
+    mul3_exact(a, dk, l);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) v[(size_t)kk * 9 + e] = l[e];
+    int p = kk + 1;
+    for (int jj = diag[k] + 1; jj < rp[k + 1]; ++jj) {
+      const int j = ci[jj];
+      while (p < end && ci[p] < j) ++p;
+      if (p == end) break;
+      if (ci[p] != j) continue;
+      double u[9], t9[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) u[e] = v[(size_t)jj * 9 + e];
+      mul3_exact(l, u, t9);
+#pragma unroll
+      for (int e = 0; e < 9; ++e) v[(size_t)p * 9 + e] = dsub(v[(size_t)p * 9 + e], t9[e]);
+    }
+  }
+  double dgl[9], inv[9];
+#pragma unroll
+  for (int e = 0; e < 9; ++e) dgl[e] = v[(size_t)diag[i] * 9 + e];
+  if (!inv3_exact(dgl, inv)) {
+    atomicMin(bad, i);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) inv[e] = 0.0;
+  }
+#pragma unroll
+  for (int e = 0; e < 9; ++e) dinv[(size_t)i * 9 + e] = inv[e];
+}
+
+// Sliced value array of one matrix from per-block values (9 doubles each),
+// vsrc = source block per slot lane (-1: padding -> 0), optional transpose.
+template <typename V>
+__global__ void k_fill_sliced(long long slots, const int *__restrict__ vsrc, int transpose,
+                              const double *__restrict__ src, V *__restrict__ out) {
+  for (long long q = blockIdx.x * (long long)kThreads + threadIdx.x; q < slots * 32;
+       q += (long long)gridDim.x * kThreads) {
+    const long long slot = q >> 5;
+    const int lane = (int)(q & 31);
+    const int sblk = vsrc[q];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
+      const double x = sblk >= 0 ? src[(size_t)sblk * 9 + ee] : 0.0;
+      out[(slot * 9 + e) * 32 + lane] = (V)x;
+    }
+  }
+}
+
+// Sliced per-row 3x3 blocks [(s*9 + e)*32 + lane] from nb*9 doubles.
+template <typename V>
+__global__ void k_fill_diag(int S, const int2 *__restrict__ srows, int transpose,
+                            const double *__restrict__ d, V *__restrict__ out) {
+  for (long long q = blockIdx.x * (long long)kThreads + threadIdx.x; q < (long long)S * 32;
+       q += (long long)gridDim.x * kThreads) {
+    const int s = (int)(q >> 5), lane = (int)(q & 31);
+    const int2 sr = srows[s];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+      const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
+      const double x = lane < sr.y ? d[(size_t)(sr.x + lane) * 9 + ee] : 0.0;
+      out[((size_t)s * 9 + e) * 32 + lane] = (V)x;
+    }
+  }
+}
+
 }  // namespace gbilu

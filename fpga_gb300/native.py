@@ -25,7 +25,8 @@ class Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("absolute_tol", C.c_int), ("device", C.c_int),
                 ("use_graph", C.c_int), ("timeout_ms", C.c_double),
                 ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
-                ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int)]
+                ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
+                ("factor_on_device", C.c_int)]
 
 
 class Result(C.Structure):
@@ -124,7 +125,7 @@ class GbIlu:
 
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
                  timeout_ms=0.0, inner_tol=1e-4, inner_maxit=500, max_outer=30,
-                 verbose=0, sweep_mode=1):
+                 verbose=0, sweep_mode=1, factor_on_device=False):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -138,6 +139,7 @@ class GbIlu:
         o.max_outer = max_outer
         o.verbose = verbose
         o.sweep_mode = sweep_mode
+        o.factor_on_device = int(factor_on_device)
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:

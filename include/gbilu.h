@@ -78,6 +78,9 @@ typedef struct {
   int sweep_mode;     /* 1: the whole ILU0 apply is one cooperative launch
                          with a grid barrier between colors (default);
                          0: one launch per color */
+  int factor_on_device; /* 1: gbilu_factor permutes and ILU0-factors on the
+                         GPU (color-parallel, bit-identical to the host
+                         factorization); 0: on the host (default) */
 } gbilu_options;
 
 typedef struct {

@@ -99,6 +99,44 @@ def test_sweep_modes_bit_identical(case):
     assert r1.half_iters == r2.half_iters and np.array_equal(x1, x2)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_factorization_bit_identical(case, precision):
+    """ILU0 on the GPU (color-parallel) gives the host/oracle factors bit for
+    bit, hence identical solves."""
+    s, P, g = case
+    with GbIlu(device=0, precision=precision, factor_on_device=True) as d, \
+            GbIlu(device=0, precision=precision) as h:
+        d.analyze(s.rowptr, s.colind).factor(s.vals)
+        h.analyze(s.rowptr, s.colind).factor(s.vals)
+        lu, dinv = d.factors()
+        assert np.array_equal(lu, P.lu) and np.array_equal(dinv, P.dinv)
+        x1, r1 = d.solve(s.b, tol=1e-8, maxit=500)
+        x2, r2 = h.solve(s.b, tol=1e-8, maxit=500)
+        assert r1.status == r2.status and np.array_equal(x1, x2)
+        # refactor with new values on the same pattern
+        v2 = s.vals * 1.5
+        d.factor(v2)
+        h.factor(v2)
+        assert np.array_equal(d.factors()[0], h.factors()[0])
+
+
+def test_device_factorization_singular(built_lib):
+    from fpga_gb300 import GbIluError
+    s = make_config("c1_20x20x10")
+    vals = s.vals.copy()
+    d = np.nonzero(s.colind[s.rowptr[10]:s.rowptr[11]] == 10)[0][0] + s.rowptr[10]
+    vals[d] = 0.0
+    msgs = []
+    for dev in (True, False):
+        with GbIlu(device=0, factor_on_device=dev) as g:
+            g.analyze(s.rowptr, s.colind)
+            with pytest.raises(GbIluError) as e:
+                g.factor(vals)
+            assert e.value.code == 7
+            msgs.append(str(e.value))
+    assert msgs[0] == msgs[1]
+
+
 def test_ilu_trace(case):
     s, P, g = case
     for transpose in (False, True):
