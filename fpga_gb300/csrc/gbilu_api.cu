@@ -99,7 +99,11 @@ struct Handle {
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][transpose]
   int per_iter[2] = {0, 0};                // launches per iteration [transpose]
   long long last_launches = 0;
-  PhaseList phases[2];                     // color steps [transpose]
+  PhaseList phases[2][2];                  // color steps [fp32][transpose]
+  StagePlan stage[2][2] = {};              // shared-memory staging of small steps
+  int stage_bytes[2][2] = {};
+  DevBuf<StageEntry> stage_tab[2][2];
+  DevBuf<int2> stage_cnt[2][2];
   cudaError_t launch_err = cudaSuccess;    // first failed cooperative launch
   int coop_grid64 = 1, coop_grid32 = 1;    // CTAs of the cooperative apply
   size_t device_bytes = 0;
@@ -144,6 +148,14 @@ int grid_for(const Handle *h, long long work) {
   return (int)std::max<long long>(1, std::min(g, cap));
 }
 
+// Kernels that end in a grid reduction: fewer, fuller CTAs, so the
+// last-CTA step sees few partials and few serialized arrival atomics.
+int reduce_grid(const Handle *h, long long work) {
+  long long g = (work + kThreads - 1) / kThreads;
+  const long long cap = (long long)h->sm_count * 2;
+  return (int)std::max<long long>(1, std::min(g, cap));
+}
+
 // ---------------------------------------------------------------------------
 // launch sequences
 // ---------------------------------------------------------------------------
@@ -154,7 +166,7 @@ void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, cons
   const Analysis &an = h->an;
   const int row0 = an.color_ptr[c], nrows = an.color_ptr[c + 1] - row0;
   if (nrows <= 0) return;
-  const long long threads = nrows <= kSmallRows ? (long long)nrows * kRowLanes : nrows;
+  const long long threads = nrows;
   k_sweep<V, T, D><<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, s>>>(
       h->ctl.p, row0, nrows, an.slice_color_ptr[c], off, col, val, dmat, src, nbr, dst);
   ++launches;
@@ -173,6 +185,7 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
     p.slice0 = an.slice_color_ptr[c];
     p.mat = mat;
     p.has_d = has_d;
+    p.staged = 0;
   };
   if (!transpose) {
     if (C == 1) {
@@ -195,10 +208,94 @@ int coop_grid(Handle *h) {
   long long most = 0;
   for (int c = 0; c < h->an.ncolors; ++c) {
     const long long rows = h->an.color_ptr[c + 1] - h->an.color_ptr[c];
-    most = std::max(most, rows <= kSmallRows ? rows * kRowLanes : rows);
+    most = std::max(most, rows);
   }
   const int need = (int)((most + kCoopThreads - 1) / kCoopThreads);
   return std::max(1, std::min(per_sm * h->sm_count, need));
+}
+
+// Shared-memory staging of the small color steps (see StageEntry): slices are
+// dealt round-robin to the CTAs of the cooperative grid; each CTA's entries
+// pack [values | column indices | D^-1] at 128-byte multiples. Staging is
+// off for this (precision, direction) when a CTA would need more than
+// kStageBudget bytes or kMaxStage entries.
+constexpr int kStageBudget = 160 * 1024;
+
+template <typename V, typename T>
+int build_stage_plan(Handle *h, int f, int t, int grid) {
+  PhaseList &pl = h->phases[f][t];
+  const Analysis &an = h->an;
+  std::vector<std::vector<StageEntry>> per(grid);
+  std::vector<long long> bytes(grid, 0);
+  for (int q = 0; q < pl.n; ++q) {
+    Phase &P = pl.p[q];
+    P.staged = 0;
+    if (P.nrows > kSmallRows) continue;
+    const SlicedMatrix &m = t == 0 ? (P.mat ? an.U : an.L) : (P.mat ? an.Lt : an.Ut);
+    const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
+    for (int j = 0; j < nsl; ++j) {
+      const int b = (j + q) % grid;
+      const int w = m.off[P.slice0 + j + 1] - m.off[P.slice0 + j];
+      const long long sz = (long long)w * 9 * 32 * sizeof(V) + (long long)w * 32 * sizeof(int) +
+                           (P.has_d ? 9 * 32 * (long long)sizeof(V) : 0);
+      per[b].push_back(StageEntry{q, j, w, (int)bytes[b]});
+      bytes[b] += sz;
+    }
+    P.staged = 1;
+  }
+  long long most = 0;
+  size_t most_n = 0;
+  for (int b = 0; b < grid; ++b) {
+    most = std::max(most, bytes[b]);
+    most_n = std::max(most_n, per[b].size());
+  }
+  h->stage[f][t] = StagePlan{nullptr, nullptr, 0};
+  h->stage_bytes[f][t] = 0;
+  if (most_n == 0 || most > kStageBudget || most_n > (size_t)kMaxStage) {
+    for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
+    return GBILU_OK;
+  }
+  std::vector<StageEntry> tab((size_t)grid * kMaxStage, StageEntry{0, 0, 0, 0});
+  std::vector<int2> cnt(grid);
+  for (int b = 0; b < grid; ++b) {
+    for (size_t e = 0; e < per[b].size(); ++e) tab[(size_t)b * kMaxStage + e] = per[b][e];
+    cnt[b] = make_int2((int)per[b].size(), (int)bytes[b]);
+  }
+  CK(h->stage_tab[f][t].alloc(tab.size()));
+  CK(h->stage_cnt[f][t].alloc(cnt.size()));
+  CK(cudaMemcpy(h->stage_tab[f][t].p, tab.data(), tab.size() * sizeof(StageEntry), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->stage_cnt[f][t].p, cnt.data(), cnt.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CK(cudaFuncSetAttribute(k_ilu_coop<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBudget));
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kCoopThreads, (size_t)most));
+  if (per_sm < 1) {
+    for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
+    return GBILU_OK;
+  }
+  h->stage[f][t] = StagePlan{h->stage_tab[f][t].p, h->stage_cnt[f][t].p, 1};
+  h->stage_bytes[f][t] = (int)most;
+  return GBILU_OK;
+}
+
+// The single-launch preconditioner apply (cooperative, all CTAs resident).
+template <typename V, typename T>
+cudaError_t launch_coop(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *hat,
+                        int trace) {
+  const int f = sizeof(T) == 4 ? 1 : 0, t = o.transpose ? 1 : 0;
+  PhaseList pl = h->phases[f][t];
+  pl.trace = trace;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.gridDim = dim3(f ? h->coop_grid32 : h->coop_grid64);
+  cfg.blockDim = dim3(kCoopThreads);
+  cfg.dynamicSmemBytes = (size_t)h->stage_bytes[f][t];
+  cfg.stream = s;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, h->stage[f][t], o.off1, o.col1,
+                            o.val1, o.off2, o.col2, o.val2, o.dmat, src, hat);
 }
 
 // hat = M^-1 src (forward) or M^-T src (transpose). In the forward case with
@@ -208,19 +305,7 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
                 int &launches) {
   const int C = h->an.ncolors;
   if (h->opt.sweep_mode == 1 && C <= kMaxPhases / 2) {
-    const PhaseList &pl = h->phases[o.transpose ? 1 : 0];
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeCooperative;
-    attr[0].val.cooperative = 1;
-    cfg.gridDim = dim3(sizeof(T) == 8 ? h->coop_grid64 : h->coop_grid32);
-    cfg.blockDim = dim3(kCoopThreads);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, o.off1, o.col1,
-                                             o.val1, o.off2, o.col2, o.val2, o.dmat, src, hat);
+    const cudaError_t e = launch_coop(h, s, o, src, hat, 0);
     if (e != cudaSuccess && h->launch_err == cudaSuccess) h->launch_err = e;
     ++launches;
     return;
@@ -273,15 +358,16 @@ void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
   Vecs<T> &w = *o.vec;
   const int n = 3 * h->an.nb, n0 = first_color_unknowns(h, o.transpose);
   const int g = grid_for(h, n);
+  const int gr = reduce_grid(h, n);
   Ctl *c = h->ctl.p;
   double *part = h->partials.p;
   apply_prec(h, s, o, w.p.p, w.ph.p, launches);
   spmv<V, T, SPMV_ALPHA>(h, s, o, w.ph.p, w.v.p, w.rt.p, launches);
-  k_update_s<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.s.p, w.sh.p, part);
+  k_update_s<T><<<gr, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.s.p, w.sh.p, part);
   apply_prec(h, s, o, w.s.p, w.sh.p, launches);
   spmv<V, T, SPMV_OMEGA>(h, s, o, w.sh.p, w.t.p, w.s.p, launches);
-  k_update_r<T><<<g, kThreads, 0, s>>>(c, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p, w.rt.p,
-                                       w.r.p, part);
+  k_update_r<T><<<gr, kThreads, 0, s>>>(c, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p, w.rt.p,
+                                        w.r.p, part);
   k_update_p<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.p.p, w.ph.p, cond);
   launches += 3;
 }
@@ -438,6 +524,13 @@ void release_device(Handle *h) {
     for (auto &g : row)
       if (g) { cudaGraphExecDestroy(g); g = nullptr; }
   for (DevMat *m : {&h->A, &h->L, &h->U, &h->At, &h->Ut, &h->Lt}) m->release();
+  for (int f = 0; f < 2; ++f)
+    for (int t = 0; t < 2; ++t) {
+      h->stage_tab[f][t].release();
+      h->stage_cnt[f][t].release();
+      h->stage[f][t] = StagePlan{nullptr, nullptr, 0};
+      h->stage_bytes[f][t] = 0;
+    }
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
   h->srows.release(); h->perm.release(); h->prowptr.release(); h->pcol.release();
@@ -505,10 +598,22 @@ int setup_device(Handle *h) {
     CK(h->dinvp.alloc((size_t)an.nb * 9));
     h->device_bytes += (size_t)an.nnzb * 9 * 16 + (size_t)an.nb * 76;
   }
-  h->phases[0] = make_phases(an, false);
-  h->phases[1] = make_phases(an, true);
+  for (int f = 0; f < 2; ++f) {
+    h->phases[f][0] = make_phases(an, false);
+    h->phases[f][1] = make_phases(an, true);
+  }
   h->coop_grid64 = coop_grid<double, double>(h);
   h->coop_grid32 = coop_grid<float, float>(h);
+  if (an.ncolors <= kMaxPhases / 2) {
+    for (int t = 0; t < 2; ++t) {
+      int rc = build_stage_plan<double, double>(h, 0, t, h->coop_grid64);
+      if (rc) return rc;
+      if (h->with_32) {
+        rc = build_stage_plan<float, float>(h, 1, t, h->coop_grid32);
+        if (rc) return rc;
+      }
+    }
+  }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
                      (size_t)an.nnzb * 8 + (size_t)an.nb * 8;
   return GBILU_OK;
@@ -609,7 +714,7 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
     // r = b - A x in FP64 with the FP64 copy of A, ||r|| read back
     k_ctl_init<<<1, 32, 0, h->st>>>(outer, 0.0, 1, 0, 0ull);
     const int S = h->an.S;
-    k_spmv<double, double, SPMV_RESID><<<(S + kWarps - 1) / kWarps, kThreads, 0, h->st>>>(
+    k_spmv<double, double, SPMV_RESID><<<std::min((S + kWarps - 1) / kWarps, 2 * h->sm_count), kThreads, 0, h->st>>>(
         outer, S, h->srows.p, o64.offA, o64.colA, o64.valA, w.x.p, w.r.p, h->b64.p, h->partials.p);
     launches += 2;
     CK(cudaMemcpyAsync(h->h_ctl, outer, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
@@ -639,7 +744,7 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
     // (staged in f.t, which the inner run overwrites only after reading it)
     k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0 / nrm, w.r.p, f.t.p);
     k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, h->opt.inner_tol, 0, h->opt.inner_maxit, tmo);
-    k_init_rhs<float><<<g, kThreads, 0, h->st>>>(h->ctl.p, n, n0, f.t.p, f.r.p, f.rt.p, f.p.p,
+    k_init_rhs<float><<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, n0, f.t.p, f.r.p, f.rt.p, f.p.p,
                                                 f.ph.p, f.x.p, h->partials.p);
     launches += 3;
     rc = run_loop<float, float>(h, transpose, h->opt.inner_maxit, launches);
@@ -1011,34 +1116,20 @@ int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows
   if (h->an.ncolors > kMaxPhases / 2) return h->fail(GBILU_BAD_INPUT, "too many colors to trace");
   CK(cudaSetDevice(h->opt.device));
   const int t = transpose ? 1 : 0;
-  PhaseList pl = h->phases[t];
-  pl.trace = 1;
+  const PhaseList &pl = h->phases[fp32 ? 1 : 0][t];
   const int n = 3 * h->an.nb;
   CK(cudaMemsetAsync(h->v64.p.p, 0, n * sizeof(double), h->st));
   if (h->with_32) CK(cudaMemsetAsync(h->v32.p.p, 0, n * sizeof(float), h->st));
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.blockDim = dim3(kCoopThreads);
-  cfg.stream = h->st;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
   for (int rep = 0; rep < 2; ++rep) {   // the second, warm run is reported
     k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
     if (fp32) {
       Ops<float, float> o = make_ops<float, float>(h, t != 0);
-      cfg.gridDim = dim3(h->coop_grid32);
       CK(cudaMemsetAsync(h->v32.ph.p, 0, n * sizeof(float), h->st));
-      CK(cudaLaunchKernelEx(&cfg, k_ilu_coop<float, float>, h->ctl.p, pl, o.off1, o.col1, o.val1,
-                            o.off2, o.col2, o.val2, o.dmat, (const float *)h->v32.p.p, h->v32.ph.p));
+      CK(launch_coop(h, h->st, o, (const float *)h->v32.p.p, h->v32.ph.p, 1));
     } else {
       Ops<double, double> o = make_ops<double, double>(h, t != 0);
-      cfg.gridDim = dim3(h->coop_grid64);
       CK(cudaMemsetAsync(h->v64.ph.p, 0, n * sizeof(double), h->st));
-      CK(cudaLaunchKernelEx(&cfg, k_ilu_coop<double, double>, h->ctl.p, pl, o.off1, o.col1,
-                            o.val1, o.off2, o.col2, o.val2, o.dmat, (const double *)h->v64.p.p,
-                            h->v64.ph.p));
+      CK(launch_coop(h, h->st, o, (const double *)h->v64.p.p, h->v64.ph.p, 1));
     }
   }
   CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));

@@ -387,60 +387,18 @@ __device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *_
   dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
 }
 
-// Colors with at most kSmallRows rows are latency-bound (a few thousand rows
-// cannot fill the GPU), so they use 8 lanes per row: lane j of the group
-// takes blocks j, j+8, ... (one memory round trip for the column, one for
-// the gather and the values), then the partial sums meet in xor shuffles.
 #ifndef GBILU_EARLY_D
 #define GBILU_EARLY_D 0
 #endif
+// Colors with at most kSmallRows rows cannot fill the GPU: their steps are
+// latency-bound and the single-launch apply stages them in shared memory.
 constexpr int kSmallRows = 16384;
-constexpr int kRowLanes = 8;
-
-// All 32 lanes of a warp call this together (rows past the end pass
-// valid = false); group g = t / 8 owns row row0 + g.
-template <typename V, typename T, bool CG>
-__device__ __forceinline__ void sweep_row8(bool valid, int row, int s, int lane, int j,
-                                           const int *__restrict__ off, const int *__restrict__ col,
-                                           const V *__restrict__ val, const V *__restrict__ dmat,
-                                           bool has_d, const T *src, const T *nbr, T *dst) {
-  T a0 = 0, a1 = 0, a2 = 0;
-  if (valid) {
-    const int o = off[s], wdt = off[s + 1] - o;
-    for (int k = j; k < wdt; k += kRowLanes) {
-      const int c = ldg_stream(col + (size_t)(o + k) * 32 + lane);
-      if (c < 0) break;
-      const V *v = val + (size_t)(o + k) * 9 * 32 + lane;
-      V bv[9];
-#pragma unroll
-      for (int e = 0; e < 9; ++e) bv[e] = ldg_stream(v + e * 32);
-      const T y0 = ldv<CG>(nbr + 3 * c), y1 = ldv<CG>(nbr + 3 * c + 1), y2 = ldv<CG>(nbr + 3 * c + 2);
-      a0 = fma(-(T)bv[0], y0, a0); a0 = fma(-(T)bv[1], y1, a0); a0 = fma(-(T)bv[2], y2, a0);
-      a1 = fma(-(T)bv[3], y0, a1); a1 = fma(-(T)bv[4], y1, a1); a1 = fma(-(T)bv[5], y2, a1);
-      a2 = fma(-(T)bv[6], y0, a2); a2 = fma(-(T)bv[7], y1, a2); a2 = fma(-(T)bv[8], y2, a2);
-    }
-  }
-#pragma unroll
-  for (int m = kRowLanes / 2; m > 0; m >>= 1) {
-    a0 += __shfl_xor_sync(0xffffffffu, a0, m);
-    a1 += __shfl_xor_sync(0xffffffffu, a1, m);
-    a2 += __shfl_xor_sync(0xffffffffu, a2, m);
-  }
-  if (valid && j == 0) {
-    a0 += ldv<CG>(src + 3 * row);
-    a1 += ldv<CG>(src + 3 * row + 1);
-    a2 += ldv<CG>(src + 3 * row + 2);
-    if (has_d) apply_d(dmat, s, lane, a0, a1, a2);
-    dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
-  }
-}
 
 // One color of a triangular sweep, one launch per color.
 // L sweep: B = L, src = p, nbr = dst = p^ (colors ascending; ilu0.vhd:413-416);
 // U sweep: B = U, D = Dinv, src = nbr = dst = p^ (colors descending;
 // ilu0.vhd:293-323,407-411). The same kernel runs the transposed sweeps of
-// the adjoint with B = U^T (D = Dinv^T) and B = L^T. Small colors
-// (nrows <= kSmallRows) are launched with 8 threads per row.
+// the adjoint with B = U^T (D = Dinv^T) and B = L^T.
 template <typename V, typename T, bool HAS_D>
 __global__ void __launch_bounds__(kThreads, 2)
 k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__ off,
@@ -448,13 +406,6 @@ k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__
         const T *src, const T *nbr, T *dst) {
   if (ctl->done) return;
   const int t = blockIdx.x * kThreads + threadIdx.x;
-  if (nrows <= kSmallRows) {
-    const int g = t / kRowLanes;
-    if ((t & ~31) / kRowLanes >= nrows) return;   // the whole warp is past the end
-    sweep_row8<V, T, false>(g < nrows, row0 + g, slice0 + (g >> 5), g & 31, t % kRowLanes, off,
-                            col, val, dmat, HAS_D, src, nbr, dst);
-    return;
-  }
   if (t >= nrows) return;
   sweep_row<V, T, false>(row0 + t, slice0 + (t >> 5), t & 31, off, col, val, dmat, HAS_D, src,
                          nbr, dst);
@@ -469,12 +420,63 @@ k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__
 // matrix 1 (U, or L^T; own rows read from hat), with or without D.
 struct Phase {
   int row0, nrows, slice0, mat, has_d;
+  int staged;                     // rows come from shared memory (see StageEntry)
 };
 struct PhaseList {
   int n;
   int trace;                      // CTA 0 stamps %globaltimer at each phase start
   Phase p[kMaxPhases];
 };
+
+// Small color steps are latency-bound: their slices (values, column
+// indices, inverse diagonal blocks) are copied into shared memory with TMA
+// bulk copies when the launch starts, so that the step itself only gathers
+// the neighbour values from L2. The host assigns slices to CTAs; entry
+// e of CTA b says: phase q, slice j of that phase's color, row width w, and
+// the byte offset pos of [values | column indices | D^-1] in shared memory.
+struct StageEntry {
+  int q, j, w, pos;
+};
+constexpr int kMaxStage = 64;         // entries per CTA
+
+struct StagePlan {
+  const StageEntry *tab;              // [grid][kMaxStage]
+  const int2 *cnt;                    // per CTA: entries, total bytes
+  int enabled;
+};
+
+constexpr unsigned int kStageSpins = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> shared bulk copy (16-byte aligned ends, size a multiple of 16),
+// completion counted on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
 
 #ifndef GBILU_COOP_THREADS
 #define GBILU_COOP_THREADS 512
@@ -520,15 +522,92 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c) {
   return ok != 0;
 }
 
+// One staged row (thread per row, data in shared memory): the column
+// indices come first so that all neighbour gathers of the row are in flight
+// together.
+template <typename V, typename T>
+__device__ __forceinline__ void staged_row(int row, int lane, int w, const V *sv, const int *sc,
+                                           const V *sd, bool has_d, const T *own, const T *nbr,
+                                           T *dst) {
+  constexpr int SB = sizeof(T) == 8 ? 4 : 8;   // gathers in flight per batch
+  T a0 = __ldcg(own + 3 * row), a1 = __ldcg(own + 3 * row + 1), a2 = __ldcg(own + 3 * row + 2);
+  for (int k0 = 0; k0 < w; k0 += SB) {
+    int c[SB];
+    T y[SB][3];
+#pragma unroll
+    for (int j = 0; j < SB; ++j) c[j] = (k0 + j < w) ? sc[(k0 + j) * 32 + lane] : -1;
+#pragma unroll
+    for (int j = 0; j < SB; ++j)
+      if (c[j] >= 0) {
+        y[j][0] = __ldcg(nbr + 3 * c[j]);
+        y[j][1] = __ldcg(nbr + 3 * c[j] + 1);
+        y[j][2] = __ldcg(nbr + 3 * c[j] + 2);
+      }
+#pragma unroll
+    for (int j = 0; j < SB; ++j)
+      if (c[j] >= 0) {
+        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + lane;
+        a0 = fma(-(T)b[0 * 32], y[j][0], a0); a0 = fma(-(T)b[1 * 32], y[j][1], a0);
+        a0 = fma(-(T)b[2 * 32], y[j][2], a0);
+        a1 = fma(-(T)b[3 * 32], y[j][0], a1); a1 = fma(-(T)b[4 * 32], y[j][1], a1);
+        a1 = fma(-(T)b[5 * 32], y[j][2], a1);
+        a2 = fma(-(T)b[6 * 32], y[j][0], a2); a2 = fma(-(T)b[7 * 32], y[j][1], a2);
+        a2 = fma(-(T)b[8 * 32], y[j][2], a2);
+      }
+  }
+  if (has_d) {
+    T dd[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) dd[e] = (T)sd[e * 32 + lane];
+    const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
+    const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
+    const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
+    a0 = z0; a1 = z1; a2 = z2;
+  }
+  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+}
+
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
 // launch, a grid barrier between consecutive steps. Vector loads go through
 // L2 because earlier steps of the same launch wrote them on other SMs.
+// Staged small steps read their matrix data from shared memory.
 template <typename V, typename T>
 __global__ void __launch_bounds__(kCoopThreads, 1)
-k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__restrict__ col1,
-           const V *__restrict__ val1, const int *__restrict__ off2, const int *__restrict__ col2,
-           const V *__restrict__ val2, const V *__restrict__ dmat, const T *src, T *hat) {
+k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
+           const int *__restrict__ col1, const V *__restrict__ val1, const int *__restrict__ off2,
+           const int *__restrict__ col2, const V *__restrict__ val2, const V *__restrict__ dmat,
+           const T *src, T *hat) {
+  extern __shared__ __align__(128) unsigned char stage_smem[];
+  __shared__ uint64_t stage_bar;
+  __shared__ StageEntry stage_tab[kMaxStage];
+  __shared__ int stage_n;
   if (ctl->done) return;
+  bool staged_ready = false;
+  if (sp.enabled) {
+    const int2 cnt = sp.cnt[blockIdx.x];
+    if (threadIdx.x == 0) {
+      stage_n = cnt.x;
+      mbar_init(&stage_bar, 1);
+      mbar_expect_tx(&stage_bar, (uint32_t)cnt.y);
+    }
+    if (threadIdx.x < cnt.x) stage_tab[threadIdx.x] = sp.tab[(size_t)blockIdx.x * kMaxStage + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < cnt.x) {
+      const StageEntry e = stage_tab[threadIdx.x];
+      const Phase P = ph.p[e.q];
+      const int s = P.slice0 + e.j;
+      const int *off = P.mat ? off2 : off1;
+      const int *col = P.mat ? col2 : col1;
+      const V *val = P.mat ? val2 : val1;
+      const size_t o = (size_t)__ldg(off + s);
+      unsigned char *dst = stage_smem + e.pos;
+      const uint32_t vb = (uint32_t)(e.w * 9 * 32 * sizeof(V)), cb = (uint32_t)(e.w * 32 * sizeof(int));
+      if (vb) bulk_g2s(dst, val + o * 9 * 32, vb, &stage_bar);
+      if (cb) bulk_g2s(dst + vb, col + o * 32, cb, &stage_bar);
+      if (P.has_d)
+        bulk_g2s(dst + vb + cb, dmat + (size_t)s * 9 * 32, (uint32_t)(9 * 32 * sizeof(V)), &stage_bar);
+    }
+  }
   const int stride = gridDim.x * kCoopThreads;
   for (int q = 0; q < ph.n; ++q) {
     if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
@@ -537,24 +616,54 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, const int *__restrict__ off1, const int *__re
     const int *col = P.mat ? col2 : col1;
     const V *val = P.mat ? val2 : val1;
     const T *own = P.mat ? hat : src;
-    if (P.nrows <= kSmallRows) {
-      const int span = ((P.nrows * kRowLanes + 31) / 32) * 32;   // whole warps
-      for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < span; t += stride) {
-        const int g = t / kRowLanes;
-        sweep_row8<V, T, true>(g < P.nrows, P.row0 + g, P.slice0 + (g >> 5), g & 31,
-                               t % kRowLanes, off, col, val, dmat, P.has_d != 0, own, hat, hat);
+    if (P.staged && sp.enabled) {
+      if (!staged_ready) {
+        // bounded wait for this CTA's bulk copies
+        unsigned int spins = 0;
+        while (!mbar_try_wait(&stage_bar, 0)) {
+          if (++spins > kStageSpins) {
+            atomicExch(&ctl->bar_fail, 2);
+            ctl->status = ST_TIMEOUT;
+            __threadfence();
+            atomicExch(&ctl->done, 1);
+            // the copies target this CTA's shared memory: give them a second
+            // bounded wait before leaving
+            for (unsigned int k = 0; k < kStageSpins && !mbar_try_wait(&stage_bar, 0); ++k) {}
+            return;
+          }
+        }
+        staged_ready = true;
+      }
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int e = warp; e < stage_n; e += kCoopThreads / 32) {
+        const StageEntry E = stage_tab[e];
+        if (E.q != q) continue;
+        const int r = 32 * E.j + lane;
+        if (r >= P.nrows) continue;
+        const V *sv = reinterpret_cast<const V *>(stage_smem + E.pos);
+        const int *sc = reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
+        const V *sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
+                                                  E.w * 32 * sizeof(int));
+        staged_row<V, T>(P.row0 + r, lane, E.w, sv, sc, sd, P.has_d != 0, own, hat, hat);
       }
     } else {
       for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < P.nrows; t += stride)
         sweep_row<V, T, true>(P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
                               P.has_d != 0, own, hat, hat);
     }
-    if (q + 1 < ph.n && !grid_barrier(ctl)) return;
-    if (ph.trace && q + 1 == ph.n) {
+    bool ok = true;
+    if (q + 1 < ph.n) ok = grid_barrier(ctl);
+    if (ok && ph.trace && q + 1 == ph.n) {
       // the end of the last phase: after every CTA finished it
-      if (!grid_barrier(ctl)) return;
-      if (blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[ph.n] = globaltimer();
+      ok = grid_barrier(ctl);
+      if (ok && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[ph.n] = globaltimer();
     }
+    if (!ok) break;
+  }
+  if (sp.enabled && !staged_ready) {
+    // no staged step ran in this CTA (e.g. the last steps were not staged):
+    // still wait, bounded, for its bulk copies before the CTA exits
+    for (unsigned int k = 0; k < kStageSpins && !mbar_try_wait(&stage_bar, 0); ++k) {}
   }
 }
 
