@@ -487,36 +487,45 @@ constexpr int kCoopThreads = GBILU_COOP_THREADS;   // one CTA per SM: half the b
 // polls marks the run failed (Ctl::bar_fail) and the kernel returns.
 constexpr unsigned int kBarrierSpins = 1u << 22;
 
-// Sense-reversing grid barrier for a cooperative launch (all CTAs resident).
-// The generation is read before arriving; the last CTA to arrive resets the
-// count and bumps the generation. Returns false after a timed-out wait.
+__device__ __forceinline__ unsigned int atom_add_release(unsigned int *p, unsigned int v) {
+  unsigned int old;
+  asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Ticket grid barrier for a cooperative launch (all CTAs resident). The
+// counter only grows: every CTA adds 1 per barrier with release semantics
+// (after bar.sync, so it publishes the whole CTA's writes) and waits with
+// acquire loads until the counter reaches the end of its round. It starts at
+// 0 per solve (k_ctl_init) and every launch that uses it has the same grid
+// size, so rounds never straddle launches. One atomic and one poll per CTA
+// instead of fence + atomic + fence + atomic. Returns false after a timed-out
+// wait.
 __device__ __forceinline__ bool grid_barrier(Ctl *c) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned int *gen = &c->bar_gen;
-    const unsigned int g = *gen;
     ok = 1;
-    __threadfence();
-    if (atomicAdd(&c->bar_count, 1u) == gridDim.x - 1) {
-      c->bar_count = 0u;
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
-      unsigned int spins = 0;
-      while (*gen == g) {
-        if (++spins > kBarrierSpins) {
-          ok = 0;
-          atomicExch(&c->bar_fail, 1);
-          c->status = ST_TIMEOUT;     // the solve stops: every later kernel
-          __threadfence();            // of the run sees done and returns
-          atomicExch(&c->done, 1);
-          break;
-        }
-        if (spins > 64) __nanosleep(32);
+    __threadfence();   // the CTA's writes (ordered by bar.sync) before the ticket
+    const unsigned int ticket = atom_add_release(&c->bar_count, 1u);
+    const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x;
+    unsigned int spins = 0;
+    while ((int)(ld_acquire(&c->bar_count) - target) < 0) {
+      if (++spins > kBarrierSpins) {
+        ok = 0;
+        atomicExch(&c->bar_fail, 1);
+        c->status = ST_TIMEOUT;     // the solve stops: every later kernel
+        __threadfence();            // of the run sees done and returns
+        atomicExch(&c->done, 1);
+        break;
       }
+      if (spins > 256) __nanosleep(32);
     }
-    __threadfence();
   }
   __syncthreads();
   return ok != 0;
