@@ -605,11 +605,13 @@ int setup_device(Handle *h) {
   h->coop_grid64 = coop_grid<double, double>(h);
   h->coop_grid32 = coop_grid<float, float>(h);
   if (an.ncolors <= kMaxPhases / 2) {
-    // FP32 only: in FP64 the staged path's registers push the big steps into
-    // spills, which costs more than staging saves
-    for (int t = 0; t < 2 && h->with_32; ++t) {
-      const int rc = build_stage_plan<float, float>(h, 1, t, h->coop_grid32);
+    for (int t = 0; t < 2; ++t) {
+      int rc = build_stage_plan<double, double>(h, 0, t, h->coop_grid64);
       if (rc) return rc;
+      if (h->with_32) {
+        rc = build_stage_plan<float, float>(h, 1, t, h->coop_grid32);
+        if (rc) return rc;
+      }
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +

@@ -230,16 +230,19 @@ template <typename V, typename T, bool NEG, bool CG>
 __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V *__restrict__ val,
                                            int o, int wdt, int lane, const T *x, T &a0, T &a1,
                                            T &a2) {
-  for (int k0 = 0; k0 < wdt; k0 += kBatch) {
-    int c[kBatch];
+  // FP64 batches of 2 keep the kernels within 128 registers (the FP64 pipe,
+  // not the load latency, bounds them); FP32 batches of kBatch
+  constexpr int B = sizeof(V) == 8 ? (kBatch < 2 ? kBatch : 2) : kBatch;
+  for (int k0 = 0; k0 < wdt; k0 += B) {
+    int c[B];
 #pragma unroll
-    for (int j = 0; j < kBatch; ++j)
+    for (int j = 0; j < B; ++j)
       c[j] = (k0 + j < wdt) ? ldg_stream(col + (size_t)(o + k0 + j) * 32 + lane) : -1;
     // all loads of the batch first ...
-    T xv[kBatch][3];
-    V b[kBatch][9];
+    T xv[B][3];
+    V b[B][9];
 #pragma unroll
-    for (int j = 0; j < kBatch; ++j) {
+    for (int j = 0; j < B; ++j) {
       if (c[j] >= 0) {
         const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
 #pragma unroll
@@ -250,7 +253,7 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
     }
     // ... then the multiply-adds
 #pragma unroll
-    for (int j = 0; j < kBatch; ++j) {
+    for (int j = 0; j < B; ++j) {
       if (c[j] >= 0) {
         T bb[9];
 #pragma unroll
@@ -260,7 +263,7 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
         a2 = fma(bb[6], xv[j][0], a2); a2 = fma(bb[7], xv[j][1], a2); a2 = fma(bb[8], xv[j][2], a2);
       }
     }
-    if (c[kBatch - 1] < 0) break;
+    if (c[B - 1] < 0) break;
   }
 }
 
