@@ -97,6 +97,7 @@ struct Handle {
   Ctl *h_ctl = nullptr;                    // pinned mirror
   bool with_t = false, with_32 = false;
   cudaGraphExec_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [fp32][transpose]
+  cudaGraphExec_t graph_ru[2] = {nullptr, nullptr};  // mixed by replacement [transpose]
   int per_iter[2] = {0, 0};                // launches per iteration [transpose]
   long long last_launches = 0;
   PhaseList phases[2][2];                  // color steps [fp32][transpose]
@@ -352,9 +353,13 @@ int first_color_unknowns(const Handle *h, bool transpose) {
 }
 
 // One full BiCGSTAB iteration (both halves, PROGRAM steps 2-17).
+// With ru64 (the FP64 operators; mixed precision by residual replacement)
+// the iteration ends with the replacement kernels, which return at once
+// unless a replacement is due.
 template <typename V, typename T>
 void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
-                       unsigned long long cond, int &launches) {
+                       unsigned long long cond, int &launches,
+                       const Ops<double, double> *ru64 = nullptr) {
   Vecs<T> &w = *o.vec;
   const int n = 3 * h->an.nb, n0 = first_color_unknowns(h, o.transpose);
   const int g = grid_for(h, n);
@@ -368,12 +373,20 @@ void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
   spmv<V, T, SPMV_OMEGA>(h, s, o, w.sh.p, w.t.p, w.s.p, launches);
   k_update_r<T><<<gr, kThreads, 0, s>>>(c, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p, w.rt.p,
                                         w.r.p, part);
+  if (ru64 && sizeof(T) == 4) {
+    Vecs<double> &d = h->v64;
+    k_ru_accumulate<<<g, kThreads, 0, s>>>(c, n, (float *)w.x.p, d.x.p, 0);
+    spmv<double, double, SPMV_TRUE>(h, s, *ru64, d.x.p, d.r.p, h->b64.p, launches);
+    k_ru_replace<<<gr, kThreads, 0, s>>>(c, n, d.r.p, (float *)w.r.p, (const float *)w.rt.p, part);
+    launches += 2;
+  }
   k_update_p<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.p.p, w.ph.p, cond);
   launches += 3;
 }
 
 template <typename V, typename T>
-int build_graph(Handle *h, const Ops<V, T> &o, cudaGraphExec_t &exec, int &per_iter) {
+int build_graph(Handle *h, const Ops<V, T> &o, cudaGraphExec_t &exec, int &per_iter,
+                const Ops<double, double> *ru64 = nullptr) {
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle cond;
@@ -389,7 +402,7 @@ int build_graph(Handle *h, const Ops<V, T> &o, cudaGraphExec_t &exec, int &per_i
   CK(cudaStreamBeginCaptureToGraph(h->cap, body, nullptr, nullptr, 0,
                                    cudaStreamCaptureModeThreadLocal));
   int launches = 0;
-  enqueue_iteration(h, h->cap, o, (unsigned long long)cond, launches);
+  enqueue_iteration(h, h->cap, o, (unsigned long long)cond, launches, ru64);
   cudaGraph_t captured = nullptr;
   CK(cudaStreamEndCapture(h->cap, &captured));
   CK(cudaGraphInstantiate(&exec, g, 0));
@@ -427,22 +440,25 @@ template <> Ops<float, float> make_ops(Handle *h, bool t) {
 // Runs the iteration loop of an already initialised Ctl (after the init
 // kernels), as a graph or host-driven, then the x fix-up.
 template <typename V, typename T>
-int run_loop(Handle *h, bool transpose, int maxit, long long &launches) {
+int run_loop(Handle *h, bool transpose, int maxit, long long &launches, bool ru = false) {
   Ops<V, T> o = make_ops<V, T>(h, transpose);
+  Ops<double, double> o64 = make_ops<double, double>(h, transpose);
+  const Ops<double, double> *ru64 = ru ? &o64 : nullptr;
   const int fp32 = sizeof(T) == 4 ? 1 : 0, ti = transpose ? 1 : 0;
   const int n = 3 * h->an.nb;
   if (h->opt.use_graph) {
-    if (!h->graph[fp32][ti]) {
-      int rc = build_graph(h, o, h->graph[fp32][ti], h->per_iter[ti]);
+    cudaGraphExec_t &gx = ru ? h->graph_ru[ti] : h->graph[fp32][ti];
+    if (!gx) {
+      int rc = build_graph(h, o, gx, h->per_iter[ti], ru64);
       if (rc) return rc;
     }
-    CK(cudaGraphLaunch(h->graph[fp32][ti], h->st));
+    CK(cudaGraphLaunch(gx, h->st));
   } else {
     // host-driven: enqueue two iterations, then look at the done flag
     for (int it = 0; it <= maxit + 1; it += 2) {
       int l = 0;
-      enqueue_iteration(h, h->st, o, 0ull, l);
-      enqueue_iteration(h, h->st, o, 0ull, l);
+      enqueue_iteration(h, h->st, o, 0ull, l, ru64);
+      enqueue_iteration(h, h->st, o, 0ull, l, ru64);
       h->per_iter[ti] = l / 2;
       launches += l;
       CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
@@ -523,6 +539,8 @@ void release_device(Handle *h) {
   for (auto &row : h->graph)
     for (auto &g : row)
       if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  for (auto &g : h->graph_ru)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
   for (DevMat *m : {&h->A, &h->L, &h->U, &h->At, &h->Ut, &h->Lt}) m->release();
   for (int f = 0; f < 2; ++f)
     for (int t = 0; t < 2; ++t) {
@@ -700,10 +718,67 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   return GBILU_OK;
 }
 
+// Mixed precision by residual replacement: FP32 storage, sweeps and
+// vectors, the FP32 correction accumulated into the FP64 x and the FP32
+// residual replaced by the FP64 b - A x whenever the recursive residual fell
+// by ru_delta (and when it reaches the bound); the stop is decided on the
+// FP64 residual. The Krylov space is never restarted. b in h->b64, x in
+// v64.x (FP64, permuted).
+int solve_mixed_ru(Handle *h, bool transpose, double tol, int maxit, gbilu_result *res,
+                   Ctl &out, long long &launches) {
+  const int n = 3 * h->an.nb;
+  Ops<double, double> o64 = make_ops<double, double>(h, transpose);
+  Vecs<double> &w = h->v64;
+  Vecs<float> &f = h->v32;
+  const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
+  k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, tol, h->opt.absolute_tol, maxit, tmo);
+  int l = 0;
+  spmv<double, double, SPMV_RESID>(h, h->st, o64, w.x.p, w.r.p, h->b64.p, l);
+  k_ru_init<<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, first_color_unknowns(h, transpose),
+                                                       h->opt.ru_delta, w.r.p, f.r.p, f.rt.p, f.p.p,
+                                                       f.ph.p, f.x.p, h->partials.p);
+  launches += l + 2;
+  int rc = run_loop<float, float>(h, transpose, maxit, launches, true);
+  if (rc) return rc;
+  // a stop after a first half owes xc += alpha p^ (k_finish_x in run_loop);
+  // then the remaining FP32 correction goes into x
+  k_ru_accumulate<<<grid_for(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, f.x.p, w.x.p, 1);
+  launches += 1;
+  CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  out = *h->h_ctl;
+  if (h->opt.use_graph) launches += (long long)out.body_runs * h->per_iter[transpose ? 1 : 0];
+  if (out.status == ST_ALREADY || (out.status == ST_NONFINITE && out.half < 0)) return GBILU_OK;
+  // report the FP64 residual of the returned x (recomputed unless the last
+  // replacement just did)
+  double tn = out.true_norm;
+  if (out.status != ST_OK) {
+    Ctl *outer = h->ctl.p + 1;
+    k_ctl_init<<<1, 32, 0, h->st>>>(outer, 0.0, 1, 0, 0ull);
+    const int S = h->an.S;
+    k_spmv<double, double, SPMV_RESID><<<std::min((S + kWarps - 1) / kWarps, 2 * h->sm_count),
+                                         kThreads, 0, h->st>>>(outer, S, h->srows.p, o64.offA,
+                                                               o64.colA, o64.valA, w.x.p, w.r.p,
+                                                               h->b64.p, h->partials.p);
+    launches += 2;
+    CK(cudaMemcpyAsync(h->h_ctl, outer, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    tn = h->h_ctl->norm0;
+  }
+  out.norm = tn;
+  if (res) {
+    res->outer_iters = out.replacements;
+    res->inner_half_iters = out.half + 1;
+    res->true_relres = out.norm0 > 0 ? tn / out.norm0 : 0.0;
+  }
+  return GBILU_OK;
+}
+
 // Mixed precision: FP32 inner BiCGSTAB inside FP64 iterative refinement.
 // b in h->b64, x in v64.x (FP64, permuted).
 int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *res,
                 Ctl &out, long long &launches) {
+  if (h->opt.mixed_scheme == 0) return solve_mixed_ru(h, transpose, tol, maxit, res, out, launches);
   const int n = 3 * h->an.nb;
   Ops<double, double> o64 = make_ops<double, double>(h, transpose);
   Vecs<double> &w = h->v64;
@@ -797,6 +872,9 @@ int gbilu_default_options(gbilu_options *o) {
   o->max_outer = 30;
   o->verbose = 0;
   o->sweep_mode = 1;
+  o->factor_on_device = 0;
+  o->mixed_scheme = 0;
+  o->ru_delta = 0.1;
   return GBILU_OK;
 }
 

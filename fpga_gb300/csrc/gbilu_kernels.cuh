@@ -45,6 +45,16 @@ struct Ctl {
   unsigned int bar_count, bar_gen;  // grid barrier of cooperative launches
   int bar_fail;                   // a barrier wait timed out
   int body_runs;                  // loop bodies run (graph launches count)
+  // mixed precision by residual replacement (reliable updates): the FP32
+  // iteration works on (quantity / sigma); x and the true residual are FP64
+  int ru_mode;                    // 1: stops are decided on the true residual
+  int ru;                         // a replacement is due at the end of this iteration
+  double sigma;                   // scale of the FP32 vectors (the initial ||r||)
+  double ru_delta;                // replace when ||r|| < ru_delta * rmax
+  double rmax;                    // largest recursive ||r|| since the last replacement
+  double rho_prev;                // rho before the last update_r (for beta after a replacement)
+  double true_norm;               // ||b - A x|| of the last replacement (FP64)
+  int replacements;
   unsigned long long phase_ns[kMaxPhases + 1];   // traced ILU apply: phase starts
 };
 
@@ -182,6 +192,14 @@ __global__ void k_ctl_init(Ctl *c, double tol, int absolute, int maxit,
     c->bar_gen = 0u;
     c->bar_fail = 0;
     c->body_runs = 0;
+    c->ru_mode = 0;
+    c->ru = 0;
+    c->sigma = 1.0;
+    c->ru_delta = 0.1;
+    c->rmax = 0.0;
+    c->rho_prev = 0.0;
+    c->true_norm = 0.0;
+    c->replacements = 0;
   }
 }
 
@@ -271,17 +289,21 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
 // sliced SpMV with fused reductions
 // --------------------------------------------------------------------------
 
-enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3 };
+enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3, SPMV_TRUE = 4 };
 
 // y = A x over all slices. RESID: y = b - A x, ||y||^2 -> init. ALPHA:
 // (y, w) -> alpha = rho/(y,w) (step 5). OMEGA: (y, w), (y, y) ->
-// omega = (y,w)/(y,y) (step 10). V: matrix value type, T: vector type.
+// omega = (y,w)/(y,y) (step 10). TRUE: y = b - A x and ||y|| into
+// Ctl::true_norm, only when a residual replacement is due.
+// V: matrix value type, T: vector type.
 template <typename V, typename T, int MODE>
 __global__ void __launch_bounds__(kThreads, 2)
 k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
        T *__restrict__ y, const T *__restrict__ w, double *partials) {
+  if (MODE == SPMV_TRUE && (!ctl->ru || ctl->done)) return;
   if (MODE != SPMV_PLAIN && MODE != SPMV_RESID && ctl->done) return;
+  constexpr bool RES = MODE == SPMV_RESID || MODE == SPMV_TRUE;
   // persistent grid: each warp walks slices warp, warp + all warps, ...;
   // one reduction per CTA at the end instead of one per 8 slices
   const int lane = threadIdx.x & 31;
@@ -295,11 +317,11 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
       const int o = off[s], wdt = off[s + 1] - o;
       T a0 = 0, a1 = 0, a2 = 0;
       row_blocks<V, T, false, false>(col, val, o, wdt, lane, x, a0, a1, a2);
-      if (MODE == SPMV_RESID) {
+      if (RES) {
         a0 = w[3 * row] - a0; a1 = w[3 * row + 1] - a1; a2 = w[3 * row + 2] - a2;
       }
       y[3 * row] = a0; y[3 * row + 1] = a1; y[3 * row + 2] = a2;
-      if (MODE == SPMV_RESID) {
+      if (RES) {
         if (sizeof(T) == 8) d1 += (double)a0 * a0 + (double)a1 * a1 + (double)a2 * a2;
         else { df_add_prod(f1, (float)a0, (float)a0); df_add_prod(f1, (float)a1, (float)a1); df_add_prod(f1, (float)a2, (float)a2); }
       } else if (MODE == SPMV_ALPHA || MODE == SPMV_OMEGA) {
@@ -320,6 +342,10 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
     double v[1] = {d1}, tot[1];
     if (grid_sum<1>(v, partials, &ctl->counter[0], tot) && threadIdx.x == 0)
       finish_init<T>(ctl, tot[0]);
+  } else if (MODE == SPMV_TRUE) {
+    double v[1] = {d1}, tot[1];
+    if (grid_sum<1>(v, partials, &ctl->counter[0], tot) && threadIdx.x == 0)
+      ctl->true_norm = sqrt(tot[0]);
   } else if (MODE == SPMV_ALPHA) {
     double v[1] = {d1}, tot[1];
     if (grid_sum<1>(v, partials, &ctl->counter[1], tot) && threadIdx.x == 0) {
@@ -742,7 +768,7 @@ k_update_s(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict
     const double ns = sqrt(tot[0]);
     push_norm(ctl, ns);
     if (!finite(ns)) stop(ctl, ST_NONFINITE, 1);
-    else if (!(ns > ctl->bound)) stop(ctl, ST_OK, 1);
+    else if (!ctl->ru_mode && !(ns > ctl->bound)) stop(ctl, ST_OK, 1);
     else if (ctl->k == ctl->maxit) stop(ctl, ST_MAXIT, 1);
     else ctl->half = 2 * ctl->k + 1;
   }
@@ -774,9 +800,18 @@ k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
     push_norm(ctl, nr);
     ctl->dots[3] = tot[1];
     if (!finite(nr)) { stop(ctl, ST_NONFINITE, 0); return; }
-    if (!(nr > ctl->bound)) { stop(ctl, ST_OK, 0); return; }
+    if (ctl->ru_mode) {
+      // the recursive residual of the FP32 iteration only schedules a
+      // replacement; the stop is decided on the true FP64 residual
+      if (!(nr > ctl->bound) || nr < ctl->ru_delta * ctl->rmax) ctl->ru = 1;
+      ctl->rmax = fmax(ctl->rmax, nr);
+    } else if (!(nr > ctl->bound)) {
+      stop(ctl, ST_OK, 0);
+      return;
+    }
     const double rho_new = tot[1];
     const double beta = (rho_new / ctl->rho) * (ctl->alpha / ctl->omega);
+    ctl->rho_prev = ctl->rho;
     ctl->rho = rho_new;
     ctl->beta = beta;
     if (ctl->omega == 0.0 || !finite(beta)) { stop(ctl, ST_BREAKDOWN, 0); return; }
@@ -786,6 +821,83 @@ k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
     }
     ctl->k += 1;
     ctl->half = 2 * ctl->k;
+  }
+}
+
+// --------------------------------------------------------------------------
+// mixed precision by residual replacement (reliable updates)
+// --------------------------------------------------------------------------
+
+// Start of a mixed solve, after the FP64 residual r64 = b - A x (k_spmv
+// RESID, which set norm0 and the bound): the FP32 iteration works on
+// r64 / sigma with sigma = ||r64||; correction xc = 0.
+__global__ void __launch_bounds__(kThreads)
+k_ru_init(Ctl *ctl, int n, int n0, double delta, const double *__restrict__ r64,
+          float *__restrict__ r, float *__restrict__ rt, float *__restrict__ p,
+          float *__restrict__ ph, float *__restrict__ xc, double *partials) {
+  if (ctl->done) return;
+  const double inv = 1.0 / ctl->norm0;
+  DF f = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const float v = (float)(r64[i] * inv);
+    r[i] = v; rt[i] = v; p[i] = v; xc[i] = 0.f;
+    if (i < n0) ph[i] = v;
+    df_add_prod(f, v, v);
+  }
+  double vv[1] = {df_value(f)}, tot[1];
+  if (grid_sum<1>(vv, partials, &ctl->counter[6], tot) && threadIdx.x == 0) {
+    ctl->ru_mode = 1;
+    ctl->ru_delta = delta;
+    ctl->sigma = ctl->norm0;
+    ctl->rho = tot[0];
+    ctl->rmax = sqrt(tot[0]);
+    ctl->true_norm = ctl->norm0;
+    ctl->bound = ctl->bound / ctl->sigma;   // recursive norms are in units of sigma
+  }
+}
+
+// Replacement, part 1: x64 += sigma * xc, xc = 0 (the FP32 correction
+// accumulated since the last replacement goes into the FP64 solution).
+__global__ void __launch_bounds__(kThreads)
+k_ru_accumulate(const Ctl *ctl, int n, float *__restrict__ xc, double *__restrict__ x64,
+                int always) {
+  if (!always && (!ctl->ru || ctl->done)) return;
+  const double sg = ctl->sigma;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    x64[i] = fma(sg, (double)xc[i], x64[i]);
+    xc[i] = 0.f;
+  }
+}
+
+// Replacement, part 3 (after r64 = b - A x64 by k_spmv in TRUE mode):
+// r = r64 / sigma; the true norm decides the stop; otherwise the FP32
+// iteration continues from the replaced residual with rho' = (r, rt) and
+// beta recomputed from it.
+__global__ void __launch_bounds__(kThreads)
+k_ru_replace(Ctl *ctl, int n, const double *__restrict__ r64, float *__restrict__ r,
+             const float *__restrict__ rt, double *partials) {
+  if (!ctl->ru || ctl->done) return;
+  const double inv = 1.0 / ctl->sigma;
+  DF f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const float v = (float)(r64[i] * inv);
+    r[i] = v;
+    df_add_prod(f1, v, v);
+    df_add_prod(f2, v, rt[i]);
+  }
+  double vv[2] = {df_value(f1), df_value(f2)}, tot[2];
+  if (grid_sum<2>(vv, partials, &ctl->counter[7], tot) && threadIdx.x == 0) {
+    ctl->ru = 0;
+    ctl->replacements += 1;
+    const double tn = ctl->true_norm;          // set by the TRUE-mode SpMV
+    push_norm(ctl, tn / ctl->sigma);
+    if (!finite(tn)) { stop(ctl, ST_NONFINITE, 0); return; }
+    if (!(tn / ctl->sigma > ctl->bound)) { stop(ctl, ST_OK, 0); return; }
+    const double rho_new = tot[1];
+    ctl->beta = (rho_new / ctl->rho_prev) * (ctl->alpha / ctl->omega);
+    ctl->rho = rho_new;
+    ctl->rmax = sqrt(tot[0]);
+    if (!finite(ctl->beta)) stop(ctl, ST_BREAKDOWN, 0);
   }
 }
 

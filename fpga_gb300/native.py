@@ -26,7 +26,8 @@ class Options(C.Structure):
                 ("use_graph", C.c_int), ("timeout_ms", C.c_double),
                 ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
                 ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
-                ("factor_on_device", C.c_int)]
+                ("factor_on_device", C.c_int), ("mixed_scheme", C.c_int),
+                ("ru_delta", C.c_double)]
 
 
 class Result(C.Structure):
@@ -125,7 +126,8 @@ class GbIlu:
 
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
                  timeout_ms=0.0, inner_tol=1e-4, inner_maxit=500, max_outer=30,
-                 verbose=0, sweep_mode=1, factor_on_device=False):
+                 verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
+                 ru_delta=0.1):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -140,6 +142,8 @@ class GbIlu:
         o.verbose = verbose
         o.sweep_mode = sweep_mode
         o.factor_on_device = int(factor_on_device)
+        o.mixed_scheme = mixed_scheme
+        o.ru_delta = ru_delta
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:

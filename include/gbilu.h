@@ -81,6 +81,12 @@ typedef struct {
   int factor_on_device; /* 1: gbilu_factor permutes and ILU0-factors on the
                          GPU (color-parallel, bit-identical to the host
                          factorization); 0: on the host (default) */
+  int mixed_scheme;   /* mixed mode: 0 (default) FP32 BiCGSTAB whose residual
+                         is replaced by the FP64 b - Ax whenever it dropped by
+                         ru_delta, x accumulated in FP64, stop on the FP64
+                         residual; 1 restarted iterative refinement (FP32
+                         inner solves to inner_tol) */
+  double ru_delta;    /* mixed scheme 0: replacement threshold (default 0.1) */
 } gbilu_options;
 
 typedef struct {
@@ -96,7 +102,8 @@ typedef struct {
   double norms[4];      /* norms[0] initial norm, [1..3] ring of the three
                            latest (bicgstab_utils.cpp:248-258) */
   int last_norm_idx;    /* index of the newest entry in norms */
-  int outer_iters;      /* mixed: refinement steps taken */
+  int outer_iters;      /* mixed: refinement steps (scheme 1) or residual
+                           replacements (scheme 0) */
   int inner_half_iters; /* mixed: inner half-iterations over all steps */
   double true_relres;   /* mixed: ||b - A x|| / ||b - A x0|| in FP64 */
   double device_ms;     /* device time of the solve (CUDA events) */

@@ -137,6 +137,26 @@ def test_device_factorization_singular(built_lib):
     assert msgs[0] == msgs[1]
 
 
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_mixed_precision_solve(case, scheme):
+    """FP32 storage/sweeps with the FP64 residual: reaches relres 1e-8 on the
+    FP64 residual; the error against the FP64 oracle solution is stated."""
+    s, P, g = case
+    x_ref, r_ref = P.solve(s.b, tol=1e-11, maxit=4000)
+    with GbIlu(device=0, precision="mixed", mixed_scheme=scheme, inner_tol=1e-3) as m:
+        m.analyze(s.rowptr, s.colind).factor(s.vals)
+        x, r = m.solve(s.b, tol=1e-8, maxit=4000)
+        x2, _ = m.solve(s.b, tol=1e-8, maxit=4000)
+    true = np.linalg.norm(s.b - s.to_scipy() @ x) / np.linalg.norm(s.b)
+    err = rel(x, x_ref)
+    print(f"mixed scheme {scheme}: status {r.status} true relres {true:.2e} "
+          f"x err vs FP64 {err:.2e} replacements/outer {r.outer_iters} halves {r.inner_half_iters}")
+    assert r.status == 0 and true <= 1e-8 * (1 + 1e-6)
+    assert abs(r.true_relres - true) <= 1e-3 * true
+    assert err < 1e-5
+    assert np.array_equal(x, x2)           # deterministic
+
+
 def test_ilu_trace(case):
     s, P, g = case
     for transpose in (False, True):
