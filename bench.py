@@ -223,17 +223,20 @@ def gpu_bench(args, world, rank, local):
     it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
     solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "spmv64_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "ilu64_c2_traffic.json")
     if os.path.exists(tfile):
         try:
             traffic = json.load(open(tfile)).get("bytes_per_launch")
         except Exception:
             traffic = None
-    dom = kern["spmv64"]
-    roofline = {"bound": "hbm", "kernel": "k_spmv<double> (BSR3 SpMV, FP64)",
+    # the dominant kernel of the FP64 solve by device-time share (ncu launch
+    # list, profiles/): the single-launch ILU0 apply
+    dom = kern["ilu64"]
+    roofline = {"bound": "hbm", "kernel": "k_ilu_coop<double> (ILU0 L+U sweeps, FP64)",
                 "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
                 "frac": dom["gbs"] / peak, "traffic": traffic,
-                "peak_kind": peak_kind, "alg_bytes_per_launch": dom["alg_bytes"]}
+                "peak_kind": peak_kind, "alg_bytes_per_launch": dom["alg_bytes"],
+                "fp64_pipe_floor_us": 9 * (st["nnzb_lower"] + st["nnzb_upper"] + st["nb"]) / 0.59e12 * 1e6}
 
     extra = {}
     if not args.quick and rank == 0:
@@ -347,6 +350,18 @@ def secondary(args, local, tol64):
     return out
 
 
+def kernel_only(args):
+    """One kernel family of the 500k-cell system timed alone (profiler target)."""
+    from fpga_gb300 import GbIlu
+    from fpga_gb300.synth import make_config
+    s = make_config(WORKLOAD)
+    g = GbIlu(device=0, precision="mixed" if args.kernel_only.endswith("32") else "fp64")
+    g.analyze(s.rowptr, s.colind).factor(s.vals)
+    ms, by, la = g.bench_kernel(args.kernel_only, reps=args.steps)
+    print(json.dumps({"kernel": args.kernel_only, "ms": ms, "alg_bytes": by, "launches": la,
+                      "gbs": by / ms / 1e6}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,7 +373,13 @@ def main():
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven launches instead of the graph loop (profiler runs: "
                          "kernels inside a conditional graph node are not listed by ncu)")
+    ap.add_argument("--kernel-only", default=None,
+                    choices=["spmv64", "ilu64", "spmv32", "ilu32"],
+                    help="time one kernel family alone (3 warm-up + --steps launches)")
     args = ap.parse_args()
+    if args.kernel_only:
+        kernel_only(args)
+        return
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         cpu_reference(args, world, rank)

@@ -778,7 +778,7 @@ int solve_mixed_ru(Handle *h, bool transpose, double tol, int maxit, gbilu_resul
 // b in h->b64, x in v64.x (FP64, permuted).
 int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *res,
                 Ctl &out, long long &launches) {
-  if (h->opt.mixed_scheme == 0) return solve_mixed_ru(h, transpose, tol, maxit, res, out, launches);
+  if (h->opt.mixed_scheme == 1) return solve_mixed_ru(h, transpose, tol, maxit, res, out, launches);
   const int n = 3 * h->an.nb;
   Ops<double, double> o64 = make_ops<double, double>(h, transpose);
   Vecs<double> &w = h->v64;
@@ -867,7 +867,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->device = 0;
   o->use_graph = 1;
   o->timeout_ms = 0.0;
-  o->inner_tol = 1e-4;
+  o->inner_tol = 1e-2;
   o->inner_maxit = 500;
   o->max_outer = 30;
   o->verbose = 0;

@@ -81,12 +81,13 @@ typedef struct {
   int factor_on_device; /* 1: gbilu_factor permutes and ILU0-factors on the
                          GPU (color-parallel, bit-identical to the host
                          factorization); 0: on the host (default) */
-  int mixed_scheme;   /* mixed mode: 0 (default) FP32 BiCGSTAB whose residual
+  int mixed_scheme;   /* mixed mode: 0 (default) iterative refinement: FP64
+                         b - Ax, FP32 inner solves of A d = r to inner_tol,
+                         x += d in FP64; 1 one FP32 BiCGSTAB run whose residual
                          is replaced by the FP64 b - Ax whenever it dropped by
                          ru_delta, x accumulated in FP64, stop on the FP64
-                         residual; 1 restarted iterative refinement (FP32
-                         inner solves to inner_tol) */
-  double ru_delta;    /* mixed scheme 0: replacement threshold (default 0.1) */
+                         residual */
+  double ru_delta;    /* mixed scheme 1: replacement threshold (default 0.1) */
 } gbilu_options;
 
 typedef struct {
@@ -102,8 +103,8 @@ typedef struct {
   double norms[4];      /* norms[0] initial norm, [1..3] ring of the three
                            latest (bicgstab_utils.cpp:248-258) */
   int last_norm_idx;    /* index of the newest entry in norms */
-  int outer_iters;      /* mixed: refinement steps (scheme 1) or residual
-                           replacements (scheme 0) */
+  int outer_iters;      /* mixed: refinement steps (scheme 0) or residual
+                           replacements (scheme 1) */
   int inner_half_iters; /* mixed: inner half-iterations over all steps */
   double true_relres;   /* mixed: ||b - A x|| / ||b - A x0|| in FP64 */
   double device_ms;     /* device time of the solve (CUDA events) */
@@ -134,7 +135,8 @@ typedef struct {
 } gbilu_stats;
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
- * no timeout, inner_tol 1e-4, inner_maxit 500, max_outer 30 */
+ * no timeout, inner_tol 1e-2, inner_maxit 500, max_outer 30, single-launch
+ * sweeps, host factorization, mixed scheme 0, ru_delta 0.1 */
 int gbilu_default_options(gbilu_options *opt);
 
 int gbilu_create(const gbilu_options *opt, void **handle);
