@@ -223,12 +223,11 @@ def gpu_bench(args, world, rank, local):
     it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
     solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "ilu64_c2_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "ilu64_c2_traffic.txt")
     if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+        for line in open(tfile):
+            if line.startswith("bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
     # the dominant kernel of the FP64 solve by device-time share (ncu launch
     # list, profiles/): the single-launch ILU0 apply
     dom = kern["ilu64"]
