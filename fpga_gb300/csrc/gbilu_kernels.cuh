@@ -756,11 +756,25 @@ k_update_s(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict
   const T alpha = (T)ctl->alpha;
   double d = 0.0;
   DF f = {0.f, 0.f};
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const T si = fma(-alpha, v[i], r[i]);
-    s[i] = si;
-    if (i < n0) sh[i] = si;
-    if (sizeof(T) == 8) d += (double)si * si; else df_add_prod(f, (float)si, (float)si);
+  const int stride = gridDim.x * kThreads;
+  // 4 elements per trip: their loads are in flight together
+  for (int i0 = blockIdx.x * kThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    T rv[4], vv4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) { rv[u] = r[i]; vv4[u] = v[i]; }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) {
+        const T si = fma(-alpha, vv4[u], rv[u]);
+        s[i] = si;
+        if (i < n0) sh[i] = si;
+        if (sizeof(T) == 8) d += (double)si * si; else df_add_prod(f, (float)si, (float)si);
+      }
+    }
   }
   if (sizeof(T) == 4) d = df_value(f);
   double vv[1] = {d}, tot[1];
@@ -785,13 +799,28 @@ k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
   const T alpha = (T)ctl->alpha, omega = (T)ctl->omega;
   double d1 = 0.0, d2 = 0.0;
   DF f1 = {0.f, 0.f}, f2 = {0.f, 0.f};
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    x[i] = fma(omega, sh[i], fma(alpha, ph[i], x[i]));
-    const T ri = fma(-omega, t[i], s[i]);
-    r[i] = ri;
-    const T rti = rt[i];
-    if (sizeof(T) == 8) { d1 += (double)ri * ri; d2 += (double)ri * rti; }
-    else { df_add_prod(f1, (float)ri, (float)ri); df_add_prod(f2, (float)ri, (float)rti); }
+  const int stride = gridDim.x * kThreads;
+  // 4 elements per trip: their loads are in flight together
+  for (int i0 = blockIdx.x * kThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    T xv[4], phv[4], shv[4], sv[4], tv[4], rtv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) {
+        xv[u] = x[i]; phv[u] = ph[i]; shv[u] = sh[i]; sv[u] = s[i]; tv[u] = t[i]; rtv[u] = rt[i];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) {
+        x[i] = fma(omega, shv[u], fma(alpha, phv[u], xv[u]));
+        const T ri = fma(-omega, tv[u], sv[u]);
+        r[i] = ri;
+        if (sizeof(T) == 8) { d1 += (double)ri * ri; d2 += (double)ri * rtv[u]; }
+        else { df_add_prod(f1, (float)ri, (float)ri); df_add_prod(f2, (float)ri, (float)rtv[u]); }
+      }
+    }
   }
   if (sizeof(T) == 4) { d1 = df_value(f1); d2 = df_value(f2); }
   double vv[2] = {d1, d2}, tot[2];
