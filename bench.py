@@ -346,7 +346,47 @@ def secondary(args, local, tol64):
                       "ratio": statistics.median(bw) / statistics.median(fw),
                       "forward_half_iters": r.half_iters, "adjoint_half_iters": ra.half_iters}
     g.close()
+    out["adjoint_mixed_2m"] = mixed_adjoint_2m(local)
     return out
+
+
+def mixed_adjoint_2m(local):
+    """200x200x50 (2M cells, 6M unknowns): mixed forward + adjoint to 1e-8,
+    time ratio, peak device memory, gradient error against the FP64 adjoint."""
+    import numpy as np
+    import torch
+    from fpga_gb300 import GbIlu
+    from fpga_gb300.synth import make_config, CONFIGS, adjoint_selection
+    c5 = CONFIGS["c5_200x200x50_mixed_adjoint"]
+    s = make_config("c5_200x200x50_mixed_adjoint")
+    cells, d = adjoint_selection(s.nb)
+    idx = (3 * cells[:, None] + np.arange(3)).reshape(-1)
+    res = {"workload": "c5_200x200x50_mixed_adjoint", "nb": s.nb, "nnzb": s.nnzb, "tol": c5["tol"]}
+    grads = {}
+    for prec in ("mixed", "fp64"):
+        torch.cuda.synchronize()
+        free0, total = torch.cuda.mem_get_info(local)
+        g = GbIlu(device=local, precision=prec)
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        x, r = g.solve(s.b, tol=c5["tol"], maxit=c5["maxit"])
+        gv = np.zeros(s.n)
+        gv[idx] = x[idx] - d
+        lam, dA, ra = g.adjoint(gv, x, tol=c5["tol"], maxit=c5["maxit"])
+        free1, _ = torch.cuda.mem_get_info(local)
+        fw = r.device_ms
+        bw = ra.device_ms
+        grads[prec] = (lam, dA)
+        res[prec] = {"forward_ms": fw, "adjoint_ms": bw, "ratio": bw / fw,
+                     "forward_status": r.status, "adjoint_status": ra.status,
+                     "forward_true_relres": r.true_relres, "adjoint_true_relres": ra.true_relres,
+                     "device_bytes_handle": g.stats()["device_bytes"],
+                     "device_bytes_measured": free0 - free1}
+        g.close()
+    res["lambda_rel_err_vs_fp64"] = float(np.linalg.norm(grads["mixed"][0] - grads["fp64"][0]) /
+                                          np.linalg.norm(grads["fp64"][0]))
+    res["dA_rel_err_vs_fp64"] = float(np.linalg.norm(grads["mixed"][1] - grads["fp64"][1]) /
+                                      np.linalg.norm(grads["fp64"][1]))
+    return res
 
 
 def kernel_only(args):

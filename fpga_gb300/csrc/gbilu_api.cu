@@ -42,18 +42,19 @@ struct DevMat {
   void release() { off.release(); col.release(); vsrc.release(); v64.release(); v32.release(); }
 };
 
-// the nine work vectors of one BiCGSTAB run
+// the work vectors of one BiCGSTAB run
 template <typename T> struct Vecs {
   DevBuf<T> x, r, rt, p, ph, v, s, sh, t;
+  DevBuf<T> y;               // first sweep of a preconditioner apply
   cudaError_t alloc(size_t n) {
-    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t}) {
+    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t, &y}) {
       cudaError_t e = b->alloc(n);
       if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
   }
   void release() {
-    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t}) b->release();
+    for (DevBuf<T> *b : {&x, &r, &rt, &p, &ph, &v, &s, &sh, &t, &y}) b->release();
   }
 };
 
@@ -161,43 +162,63 @@ int reduce_grid(const Handle *h, long long work) {
 // launch sequences
 // ---------------------------------------------------------------------------
 
-template <typename V, typename T, bool D>
-void sweep_color(Handle *h, cudaStream_t s, const int *off, const int *col, const V *val,
-                 const V *dmat, int c, const T *src, const T *nbr, T *dst, int &launches) {
-  const Analysis &an = h->an;
-  const int row0 = an.color_ptr[c], nrows = an.color_ptr[c + 1] - row0;
-  if (nrows <= 0) return;
-  const long long threads = nrows;
-  k_sweep<V, T, D><<<(unsigned)((threads + kThreads - 1) / kThreads), kThreads, 0, s>>>(
-      h->ctl.p, row0, nrows, an.slice_color_ptr[c], off, col, val, dmat, src, nbr, dst);
-  ++launches;
-}
-
 // The color steps of one preconditioner apply, in execution order.
+// Forward (z = U^-1 L^-1 src): the L sweep over colors 1..C-1 writes y for
+// every row (color 0's y is src itself) and the final z = D^-1 y for the
+// rows without a higher-colored neighbour; the U sweep then covers color 0
+// and the leading rows of colors C-2..1. Transposed (z = L^-T U^-T src): the
+// U^T sweep with D^-T over all colors, the rows without a higher-colored
+// neighbour final at once (unit diagonal of L^T); the L^T sweep covers the
+// leading rows of colors C-2..0.
 PhaseList make_phases(const Analysis &an, bool transpose) {
   PhaseList pl;
   pl.n = 0;
   pl.trace = 0;
   const int C = an.ncolors;
-  auto add = [&](int c, int mat, int has_d) {
+  auto rows = [&](int c) { return an.color_ptr[c + 1] - an.color_ptr[c]; };
+  auto add = [&](int c, int mat, int nrows) -> Phase & {
     Phase &p = pl.p[pl.n++];
+    p = Phase{};
     p.row0 = an.color_ptr[c];
-    p.nrows = an.color_ptr[c + 1] - an.color_ptr[c];
+    p.nrows = nrows;
     p.slice0 = an.slice_color_ptr[c];
     p.mat = mat;
-    p.has_d = has_d;
-    p.staged = 0;
+    return p;
   };
   if (!transpose) {
-    if (C == 1) {
-      add(0, 0, 1);
-    } else {
-      for (int c = 1; c < C; ++c) add(c, 0, c == C - 1);
-      for (int c = C - 2; c >= 0; --c) add(c, 1, 1);
+    if (C == 1) {   // no couplings: z = D^-1 src
+      add(0, 1, rows(0)).has_d = 1;
+      return pl;
+    }
+    for (int c = 1; c < C; ++c) {
+      Phase &p = add(c, 0, rows(c));
+      p.src_rows = an.color_ptr[1];
+      p.to_y = 1;
+      p.final0 = an.color_ptr[c] + an.split[c];
+      p.final_d = 1;
+    }
+    for (int c = C - 2; c >= 0; --c) {
+      const int nr = c == 0 ? rows(0) : an.split[c];
+      if (nr == 0) continue;
+      Phase &p = add(c, 1, nr);
+      p.has_d = 1;
+      p.own_y = c == 0 ? 0 : 1;
+      p.nbr_hat = 1;
     }
   } else {
-    for (int c = 0; c < C; ++c) add(c, 0, 1);
-    for (int c = C - 2; c >= 0; --c) add(c, 1, 0);
+    for (int c = 0; c < C; ++c) {
+      Phase &p = add(c, 0, rows(c));
+      p.has_d = 1;
+      p.to_y = 1;
+      p.final0 = an.color_ptr[c] + an.split[c];
+      p.final_d = 0;
+    }
+    for (int c = C - 2; c >= 0; --c) {
+      if (an.split[c] == 0) continue;
+      Phase &p = add(c, 1, an.split[c]);
+      p.own_y = 1;
+      p.nbr_hat = 1;
+    }
   }
   return pl;
 }
@@ -238,7 +259,7 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
       const int b = (j + q) % grid;
       const int w = m.off[P.slice0 + j + 1] - m.off[P.slice0 + j];
       const long long sz = (long long)w * 9 * 32 * sizeof(V) + (long long)w * 32 * sizeof(int) +
-                           (P.has_d ? 9 * 32 * (long long)sizeof(V) : 0);
+                           (P.uses_d() ? 9 * 32 * (long long)sizeof(V) : 0);
       per[b].push_back(StageEntry{q, j, w, (int)bytes[b]});
       bytes[b] += sz;
     }
@@ -296,11 +317,11 @@ cudaError_t launch_coop(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   return cudaLaunchKernelEx(&cfg, k_ilu_coop<V, T>, h->ctl.p, pl, h->stage[f][t], o.off1, o.col1,
-                            o.val1, o.off2, o.col2, o.val2, o.dmat, src, hat);
+                            o.val1, o.off2, o.col2, o.val2, o.dmat, src, o.vec->y.p, hat);
 }
 
-// hat = M^-1 src (forward) or M^-T src (transpose). In the forward case with
-// two or more colors, hat must already hold src on color 0's unknowns.
+// hat = M^-1 src (forward) or M^-T src (transpose); the vector set's y holds
+// the first sweep's result.
 template <typename V, typename T>
 void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *hat,
                 int &launches) {
@@ -311,26 +332,13 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
     ++launches;
     return;
   }
-  if (!o.transpose) {
-    if (C == 1) {
-      sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, 0, src, hat, hat, launches);
-      return;
-    }
-    for (int c = 1; c < C; ++c) {
-      if (c == C - 1)   // the last color has no U blocks: fuse its D^-1
-        sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
-      else
-        sweep_color<V, T, false>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
-    }
-    for (int c = C - 2; c >= 0; --c)
-      sweep_color<V, T, true>(h, s, o.off2, o.col2, o.val2, o.dmat, c, hat, hat, hat, launches);
-  } else {
-    // U^T w = src forward over colors (diagonal blocks U_ii^T), then
-    // L^T z = w backward (unit diagonal); the last color's L^T rows are empty
-    for (int c = 0; c < C; ++c)
-      sweep_color<V, T, true>(h, s, o.off1, o.col1, o.val1, o.dmat, c, src, hat, hat, launches);
-    for (int c = C - 2; c >= 0; --c)
-      sweep_color<V, T, false>(h, s, o.off2, o.col2, o.val2, o.dmat, c, hat, hat, hat, launches);
+  const PhaseList &pl = h->phases[sizeof(T) == 4 ? 1 : 0][o.transpose ? 1 : 0];
+  for (int q = 0; q < pl.n; ++q) {
+    const Phase &P = pl.p[q];
+    k_phase<V, T><<<(unsigned)((P.nrows + kThreads - 1) / kThreads), kThreads, 0, s>>>(
+        h->ctl.p, P, P.mat ? o.off2 : o.off1, P.mat ? o.col2 : o.col1, P.mat ? o.val2 : o.val1,
+        o.dmat, src, o.vec->y.p, hat);
+    ++launches;
   }
 }
 
@@ -346,12 +354,6 @@ void spmv(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *x, T *y, const
   ++launches;
 }
 
-// unknowns of color 0 that the producers copy into the preconditioned vector
-int first_color_unknowns(const Handle *h, bool transpose) {
-  if (transpose || h->an.ncolors < 2) return 0;
-  return 3 * h->an.color_ptr[1];
-}
-
 // One full BiCGSTAB iteration (both halves, PROGRAM steps 2-17).
 // With ru64 (the FP64 operators; mixed precision by residual replacement)
 // the iteration ends with the replacement kernels, which return at once
@@ -361,14 +363,14 @@ void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
                        unsigned long long cond, int &launches,
                        const Ops<double, double> *ru64 = nullptr) {
   Vecs<T> &w = *o.vec;
-  const int n = 3 * h->an.nb, n0 = first_color_unknowns(h, o.transpose);
+  const int n = 3 * h->an.nb;
   const int g = grid_for(h, n);
   const int gr = reduce_grid(h, n);
   Ctl *c = h->ctl.p;
   double *part = h->partials.p;
   apply_prec(h, s, o, w.p.p, w.ph.p, launches);
   spmv<V, T, SPMV_ALPHA>(h, s, o, w.ph.p, w.v.p, w.rt.p, launches);
-  k_update_s<T><<<gr, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.s.p, w.sh.p, part);
+  k_update_s<T><<<gr, kThreads, 0, s>>>(c, n, w.r.p, w.v.p, w.s.p, part);
   apply_prec(h, s, o, w.s.p, w.sh.p, launches);
   spmv<V, T, SPMV_OMEGA>(h, s, o, w.sh.p, w.t.p, w.s.p, launches);
   k_update_r<T><<<gr, kThreads, 0, s>>>(c, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p, w.rt.p,
@@ -380,7 +382,7 @@ void enqueue_iteration(Handle *h, cudaStream_t s, const Ops<V, T> &o,
     k_ru_replace<<<gr, kThreads, 0, s>>>(c, n, d.r.p, (float *)w.r.p, (const float *)w.rt.p, part);
     launches += 2;
   }
-  k_update_p<T><<<g, kThreads, 0, s>>>(c, n, n0, w.r.p, w.v.p, w.p.p, w.ph.p, cond);
+  k_update_p<T><<<g, kThreads, 0, s>>>(c, n, w.r.p, w.v.p, w.p.p, cond);
   launches += 3;
 }
 
@@ -707,7 +709,7 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   spmv<double, double, SPMV_RESID>(h, h->st, o, w.x.p, w.r.p, h->b64.p, l);
   launches += l;
   k_init_vectors<double><<<grid_for(h, n), kThreads, 0, h->st>>>(
-      h->ctl.p, n, first_color_unknowns(h, transpose), w.r.p, w.rt.p, w.p.p, w.ph.p);
+      h->ctl.p, n, w.r.p, w.rt.p, w.p.p);
   launches += 1;
   int rc = run_loop<double, double>(h, transpose, maxit, launches);
   if (rc) return rc;
@@ -734,9 +736,8 @@ int solve_mixed_ru(Handle *h, bool transpose, double tol, int maxit, gbilu_resul
   k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, tol, h->opt.absolute_tol, maxit, tmo);
   int l = 0;
   spmv<double, double, SPMV_RESID>(h, h->st, o64, w.x.p, w.r.p, h->b64.p, l);
-  k_ru_init<<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, first_color_unknowns(h, transpose),
-                                                       h->opt.ru_delta, w.r.p, f.r.p, f.rt.p, f.p.p,
-                                                       f.ph.p, f.x.p, h->partials.p);
+  k_ru_init<<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, h->opt.ru_delta, w.r.p, f.r.p,
+                                                       f.rt.p, f.p.p, f.x.p, h->partials.p);
   launches += l + 2;
   int rc = run_loop<float, float>(h, transpose, maxit, launches, true);
   if (rc) return rc;
@@ -812,15 +813,14 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
     return GBILU_OK;
   }
   const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
-  const int n0 = first_color_unknowns(h, transpose);
   int outer_steps = 0, inner_half = 0;
   while (nrm > bound && outer_steps < h->opt.max_outer) {
     // right-hand side of the correction equation A d = r / ||r|| in FP32
     // (staged in f.t, which the inner run overwrites only after reading it)
     k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0 / nrm, w.r.p, f.t.p);
     k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, h->opt.inner_tol, 0, h->opt.inner_maxit, tmo);
-    k_init_rhs<float><<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, n0, f.t.p, f.r.p, f.rt.p, f.p.p,
-                                                f.ph.p, f.x.p, h->partials.p);
+    k_init_rhs<float><<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, f.t.p, f.r.p, f.rt.p,
+                                                                 f.p.p, f.x.p, h->partials.p);
     launches += 3;
     rc = run_loop<float, float>(h, transpose, h->opt.inner_maxit, launches);
     if (rc) return rc;
@@ -1111,8 +1111,6 @@ int gbilu_apply_ilu(void *handle, const double *p, double *z, int transpose) {
   k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
   CK(cudaMemcpyAsync(h->io64.p, p, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64.p, w.p.p, 1.0);
-  const int n0 = first_color_unknowns(h, t);
-  if (n0) CK(cudaMemcpyAsync(w.ph.p, w.p.p, n0 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   apply_prec(h, h->st, o, w.p.p, w.ph.p, launches);
   k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, w.ph.p, h->io64b.p);
   CK(cudaMemcpyAsync(z, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -1171,14 +1169,14 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   s->analyze_ms = h->analyze_ms;
   for (int p = 0; p < 2; ++p) {
     const double sv = p ? 4.0 : 8.0, sx = sv, si = 4.0;
-    const double nb = an.nb, n = 3.0 * an.nb, n0 = first_color_unknowns(h, false);
+    const double nb = an.nb, n = 3.0 * an.nb;
     const double nlu = (double)an.nnzb_l + an.nnzb_u;
     s->alg_bytes_spmv[p] = an.nnzb * (9 * sv + si) + (nb + 1) * si + 2 * n * sx;
     s->alg_bytes_ilu[p] = nlu * (9 * sv + si) + 2 * (nb + 1) * si + nb * 9 * sv + 4 * n * sx;
-    // fused vector kernels of one iteration: update_s (r, v -> s, s^[c0]),
-    // update_r (x, p^, s^, s, t, rt -> x, r), update_p (r, v, p -> p, p^[c0])
+    // fused vector kernels of one iteration: update_s (r, v -> s),
+    // update_r (x, p^, s^, s, t, rt -> x, r), update_p (r, v, p -> p)
     // and the dot operands of the two SpMV epilogues (rt, s)
-    const double vec = (17.0 * n + 2.0 * n0) * sx;
+    const double vec = 17.0 * n * sx;
     s->alg_bytes_iter[p] = 2 * s->alg_bytes_spmv[p] + 2 * s->alg_bytes_ilu[p] + vec;
   }
   return GBILU_OK;
@@ -1233,7 +1231,6 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   gbilu_stats st;
   gbilu_get_stats(h, &st);
   const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
-  const int n0 = first_color_unknowns(h, false);
   int launches = 0;
   k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, 0.0, 0, 0, 0ull);
   // inputs: a fixed pseudo-random vector in the permuted numbering
@@ -1245,11 +1242,6 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   }
   CK(cudaMemcpyAsync(h->v64.p.p, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   if (h->with_32) k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0, h->v64.p.p, h->v32.p.p);
-  if (n0) {
-    CK(cudaMemcpyAsync(h->v64.ph.p, h->v64.p.p, n0 * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-    if (h->with_32)
-      CK(cudaMemcpyAsync(h->v32.ph.p, h->v32.p.p, n0 * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-  }
   auto run = [&](int &l) {
     if (which == 0) {
       Ops<double, double> o = make_ops<double, double>(h, false);

@@ -36,6 +36,8 @@ struct Analysis {
   std::vector<int> color;                 // [nb] color of input row
   std::vector<int> perm, iperm;           // perm[new] = old
   std::vector<int> color_ptr;             // [C+1] new-index range per color
+  std::vector<int> split;                 // [C] leading rows of a color with a
+                                          // higher-colored neighbour
   std::vector<int> prowptr, pcolind;      // permuted pattern, sorted columns
   std::vector<int> psrc;                  // permuted block -> input block
   std::vector<int> pdiag;                 // position of the diagonal block

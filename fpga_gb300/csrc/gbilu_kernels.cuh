@@ -244,10 +244,12 @@ template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p) {
 // coalesced value loads of kBatch blocks are in flight together: a row of
 // w blocks costs about 2*ceil(w/kBatch) memory round trips instead of 2*w.
 // Padding slots (column -1) only occur after a row's last block.
+// Neighbour columns below lo are read from xlo instead of x (the first sweep
+// reads the input vector for color 0, whose L rows are empty).
 template <typename V, typename T, bool NEG, bool CG>
 __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V *__restrict__ val,
-                                           int o, int wdt, int lane, const T *x, T &a0, T &a1,
-                                           T &a2) {
+                                           int o, int wdt, int lane, const T *x, const T *xlo,
+                                           int lo, T &a0, T &a1, T &a2) {
   // FP64 batches of 2 keep the kernels within 128 registers (the FP64 pipe,
   // not the load latency, bounds them); FP32 batches of kBatch
   constexpr int B = sizeof(V) == 8 ? (kBatch < 2 ? kBatch : 2) : kBatch;
@@ -263,8 +265,9 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
     for (int j = 0; j < B; ++j) {
       if (c[j] >= 0) {
         const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
+        const T *xs = c[j] < lo ? xlo : x;
 #pragma unroll
-        for (int e = 0; e < 3; ++e) xv[j][e] = ldv<CG>(x + 3 * c[j] + e);
+        for (int e = 0; e < 3; ++e) xv[j][e] = ldv<CG>(xs + 3 * c[j] + e);
 #pragma unroll
         for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
       }
@@ -316,7 +319,7 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
       const int row = sr.x + lane;
       const int o = off[s], wdt = off[s + 1] - o;
       T a0 = 0, a1 = 0, a2 = 0;
-      row_blocks<V, T, false, false>(col, val, o, wdt, lane, x, a0, a1, a2);
+      row_blocks<V, T, false, false>(col, val, o, wdt, lane, x, x, 0, a0, a1, a2);
       if (RES) {
         a0 = w[3 * row] - a0; a1 = w[3 * row + 1] - a1; a2 = w[3 * row + 2] - a2;
       }
@@ -371,86 +374,90 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
 // one color of a triangular sweep
 // --------------------------------------------------------------------------
 
-// D multiply of one row: (a0, a1, a2) <- D_s,lane (a0, a1, a2)
-template <typename V, typename T>
-__device__ __forceinline__ void apply_d(const V *__restrict__ dmat, int s, int lane, T &a0, T &a1,
-                                        T &a2) {
-  const V *d = dmat + (size_t)s * 9 * 32 + lane;
+// One color step of a preconditioner apply: rows [row0, row0 + nrows)
+// starting at slice slice0 of matrix mat (0: L, or U^T in the adjoint; 1: U,
+// or L^T). The first sweep (L forward; U^T in the adjoint) writes its result
+// y to ybuf for every row of the color, and for the rows from final0 on --
+// those with no neighbour of a higher color, ordered last in their color --
+// the final value hat = [D] y right away. The second sweep (U backward; L^T)
+// then only covers the leading rows of each color: hat = [D] (ybuf - B hat).
+// Color 0 has no L rows: its y is the input itself (src).
+// L sweep: ilu0.vhd:413-416, colors ascending (sparstition.vhd:751-756);
+// U sweep with D^-1: ilu0.vhd:293-323,407-411, colors descending.
+struct Phase {
+  int row0, nrows, slice0, mat;
+  int has_d;      // D applied to the row result (the adjoint's U^T step: D^-T)
+  int own_y;      // own rows read ybuf (second sweep) instead of src
+  int nbr_hat;    // neighbours read hat (second sweep) instead of ybuf
+  int src_rows;   // first sweep: neighbour rows below this read src (color 0)
+  int to_y;       // first sweep: the result goes to ybuf ...
+  int final0;     // ... and rows from final0 on are final: hat = [D] result
+  int final_d;    //     with D = D^-1 (forward) or the identity (adjoint)
+  int staged;     // the step's matrix rows come from shared memory
+  // whether a D block of the step's rows is read
+  __host__ __device__ bool uses_d() const { return has_d || (to_y && final_d); }
+};
+
+// (a0, a1, a2) <- D (a0, a1, a2) with D at d[e*32], e = 0..8 (row-major)
+template <typename V, typename T, bool GLOBAL>
+__device__ __forceinline__ void apply_dp(const V *d, T &a0, T &a1, T &a2) {
   T dd[9];
 #pragma unroll
-  for (int e = 0; e < 9; ++e) dd[e] = (T)ldg_stream(d + e * 32);
+  for (int e = 0; e < 9; ++e) dd[e] = GLOBAL ? (T)ldg_stream(d + e * 32) : (T)d[e * 32];
   const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
   const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
   const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
   a0 = z0; a1 = z1; a2 = z2;
 }
 
-// One row of a sweep, one thread: dst_i = [D_i] (src_i - sum_j B_ij nbr_j).
-template <typename V, typename T, bool CG>
-__device__ __forceinline__ void sweep_row(int row, int s, int lane, const int *__restrict__ off,
-                                          const int *__restrict__ col, const V *__restrict__ val,
-                                          const V *__restrict__ dmat, bool has_d, const T *src,
-                                          const T *nbr, T *dst) {
-  const int o = off[s], wdt = off[s + 1] - o;
-  T a0 = ldv<CG>(src + 3 * row), a1 = ldv<CG>(src + 3 * row + 1), a2 = ldv<CG>(src + 3 * row + 2);
-#if GBILU_EARLY_D
-  // the inverse diagonal block does not depend on the row's columns: load it
-  // before the column chain so that it arrives with the first batch
-  V dd[9];
-  if (has_d) {
-    const V *d = dmat + (size_t)s * 9 * 32 + lane;
-#pragma unroll
-    for (int e = 0; e < 9; ++e) dd[e] = ldg_stream(d + e * 32);
+// Stores one row's result as the phase says (d: this row's D block).
+template <typename V, typename T, bool GLOBAL>
+__device__ __forceinline__ void phase_store(const Phase &P, int row, const V *d, T a0, T a1,
+                                            T a2, T *ybuf, T *hat) {
+  if (P.has_d) apply_dp<V, T, GLOBAL>(d, a0, a1, a2);
+  if (P.to_y) {
+    ybuf[3 * row] = a0; ybuf[3 * row + 1] = a1; ybuf[3 * row + 2] = a2;
+    if (row < P.final0) return;
+    if (P.final_d) apply_dp<V, T, GLOBAL>(d, a0, a1, a2);
   }
-  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
-  if (has_d) {
-    const T z0 = (T)dd[0] * a0 + (T)dd[1] * a1 + (T)dd[2] * a2;
-    const T z1 = (T)dd[3] * a0 + (T)dd[4] * a1 + (T)dd[5] * a2;
-    const T z2 = (T)dd[6] * a0 + (T)dd[7] * a1 + (T)dd[8] * a2;
-    a0 = z0; a1 = z1; a2 = z2;
-  }
-#else
-  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, nbr, a0, a1, a2);
-  if (has_d) apply_d(dmat, s, lane, a0, a1, a2);
-#endif
-  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+  hat[3 * row] = a0; hat[3 * row + 1] = a1; hat[3 * row + 2] = a2;
 }
 
-#ifndef GBILU_EARLY_D
-#define GBILU_EARLY_D 0
-#endif
+// One row of a step, one thread: a = own_i - sum_j B_ij nbr_j, then stored.
+template <typename V, typename T, bool CG>
+__device__ __forceinline__ void phase_row(const Phase &P, int row, int s, int lane,
+                                          const int *__restrict__ off, const int *__restrict__ col,
+                                          const V *__restrict__ val, const V *__restrict__ dmat,
+                                          const T *src, T *ybuf, T *hat) {
+  const T *own = P.own_y ? ybuf : src;
+  const int o = off[s], wdt = off[s + 1] - o;
+  T a0 = ldv<CG>(own + 3 * row), a1 = ldv<CG>(own + 3 * row + 1), a2 = ldv<CG>(own + 3 * row + 2);
+  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, P.nbr_hat ? hat : ybuf, src, P.src_rows, a0,
+                             a1, a2);
+  phase_store<V, T, true>(P, row, dmat + (size_t)s * 9 * 32 + lane, a0, a1, a2, ybuf, hat);
+}
+
 // Colors with at most kSmallRows rows cannot fill the GPU: their steps are
 // latency-bound and the single-launch apply stages them in shared memory.
 constexpr int kSmallRows = 16384;
 
-// One color of a triangular sweep, one launch per color.
-// L sweep: B = L, src = p, nbr = dst = p^ (colors ascending; ilu0.vhd:413-416);
-// U sweep: B = U, D = Dinv, src = nbr = dst = p^ (colors descending;
-// ilu0.vhd:293-323,407-411). The same kernel runs the transposed sweeps of
-// the adjoint with B = U^T (D = Dinv^T) and B = L^T.
-template <typename V, typename T, bool HAS_D>
+// One step per launch (the per-color mode; the same row arithmetic as the
+// single-launch apply, so both give identical bits).
+template <typename V, typename T>
 __global__ void __launch_bounds__(kThreads, 2)
-k_sweep(const Ctl *ctl, int row0, int nrows, int slice0, const int *__restrict__ off,
-        const int *__restrict__ col, const V *__restrict__ val, const V *__restrict__ dmat,
-        const T *src, const T *nbr, T *dst) {
+k_phase(const Ctl *ctl, Phase P, const int *__restrict__ off, const int *__restrict__ col,
+        const V *__restrict__ val, const V *__restrict__ dmat, const T *src, T *ybuf, T *hat) {
   if (ctl->done) return;
   const int t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= nrows) return;
-  sweep_row<V, T, false>(row0 + t, slice0 + (t >> 5), t & 31, off, col, val, dmat, HAS_D, src,
-                         nbr, dst);
+  if (t >= P.nrows) return;
+  phase_row<V, T, false>(P, P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat, src,
+                         ybuf, hat);
 }
 
 // --------------------------------------------------------------------------
 // whole preconditioner apply in one cooperative launch
 // --------------------------------------------------------------------------
 
-// One color step of a sweep: rows [row0, row0+nrows) starting at slice
-// slice0, matrix 0 (L, or U^T in the adjoint; own rows read from src) or
-// matrix 1 (U, or L^T; own rows read from hat), with or without D.
-struct Phase {
-  int row0, nrows, slice0, mat, has_d;
-  int staged;                     // rows come from shared memory (see StageEntry)
-};
 struct PhaseList {
   int n;
   int trace;                      // CTA 0 stamps %globaltimer at each phase start
@@ -562,12 +569,14 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c) {
 
 // One staged row (thread per row, data in shared memory): the column
 // indices come first so that all neighbour gathers of the row are in flight
-// together.
+// together. Same arithmetic as phase_row.
 template <typename V, typename T>
-__device__ __forceinline__ void staged_row(int row, int lane, int w, const V *sv, const int *sc,
-                                           const V *sd, bool has_d, const T *own, const T *nbr,
-                                           T *dst) {
+__device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, int w, const V *sv,
+                                           const int *sc, const V *sd, const T *src, T *ybuf,
+                                           T *hat) {
   constexpr int SB = sizeof(T) == 8 ? 4 : 8;   // gathers in flight per batch
+  const T *own = P.own_y ? ybuf : src;
+  const T *nbr = P.nbr_hat ? hat : ybuf;
   T a0 = __ldcg(own + 3 * row), a1 = __ldcg(own + 3 * row + 1), a2 = __ldcg(own + 3 * row + 2);
   for (int k0 = 0; k0 < w; k0 += SB) {
     int c[SB];
@@ -577,9 +586,10 @@ __device__ __forceinline__ void staged_row(int row, int lane, int w, const V *sv
 #pragma unroll
     for (int j = 0; j < SB; ++j)
       if (c[j] >= 0) {
-        y[j][0] = __ldcg(nbr + 3 * c[j]);
-        y[j][1] = __ldcg(nbr + 3 * c[j] + 1);
-        y[j][2] = __ldcg(nbr + 3 * c[j] + 2);
+        const T *xs = c[j] < P.src_rows ? src : nbr;
+        y[j][0] = __ldcg(xs + 3 * c[j]);
+        y[j][1] = __ldcg(xs + 3 * c[j] + 1);
+        y[j][2] = __ldcg(xs + 3 * c[j] + 2);
       }
 #pragma unroll
     for (int j = 0; j < SB; ++j)
@@ -593,16 +603,7 @@ __device__ __forceinline__ void staged_row(int row, int lane, int w, const V *sv
         a2 = fma(-(T)b[8 * 32], y[j][2], a2);
       }
   }
-  if (has_d) {
-    T dd[9];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) dd[e] = (T)sd[e * 32 + lane];
-    const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
-    const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
-    const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
-    a0 = z0; a1 = z1; a2 = z2;
-  }
-  dst[3 * row] = a0; dst[3 * row + 1] = a1; dst[3 * row + 2] = a2;
+  phase_store<V, T, false>(P, row, sd + lane, a0, a1, a2, ybuf, hat);
 }
 
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
@@ -614,7 +615,7 @@ __global__ void __launch_bounds__(kCoopThreads, 1)
 k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
            const int *__restrict__ col1, const V *__restrict__ val1, const int *__restrict__ off2,
            const int *__restrict__ col2, const V *__restrict__ val2, const V *__restrict__ dmat,
-           const T *src, T *hat) {
+           const T *src, T *ybuf, T *hat) {
   extern __shared__ __align__(128) unsigned char stage_smem[];
   __shared__ uint64_t stage_bar;
   __shared__ StageEntry stage_tab[kMaxStage];
@@ -642,7 +643,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       const uint32_t vb = (uint32_t)(e.w * 9 * 32 * sizeof(V)), cb = (uint32_t)(e.w * 32 * sizeof(int));
       if (vb) bulk_g2s(dst, val + o * 9 * 32, vb, &stage_bar);
       if (cb) bulk_g2s(dst + vb, col + o * 32, cb, &stage_bar);
-      if (P.has_d)
+      if (P.uses_d())
         bulk_g2s(dst + vb + cb, dmat + (size_t)s * 9 * 32, (uint32_t)(9 * 32 * sizeof(V)), &stage_bar);
     }
   }
@@ -653,7 +654,6 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
     const int *off = P.mat ? off2 : off1;
     const int *col = P.mat ? col2 : col1;
     const V *val = P.mat ? val2 : val1;
-    const T *own = P.mat ? hat : src;
     if (P.staged && sp.enabled) {
       if (!staged_ready) {
         // bounded wait for this CTA's bulk copies
@@ -682,12 +682,12 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         const int *sc = reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
         const V *sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
                                                   E.w * 32 * sizeof(int));
-        staged_row<V, T>(P.row0 + r, lane, E.w, sv, sc, sd, P.has_d != 0, own, hat, hat);
+        staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
       }
     } else {
       for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < P.nrows; t += stride)
-        sweep_row<V, T, true>(P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
-                              P.has_d != 0, own, hat, hat);
+        phase_row<V, T, true>(P, P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
+                              src, ybuf, hat);
     }
     bool ok = true;
     if (q + 1 < ph.n) ok = grid_barrier(ctl);
@@ -709,18 +709,16 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
 // fused vector kernels (grid-stride over the n unknowns)
 // --------------------------------------------------------------------------
 
-// After step 1: rt = p = r; p^ = r on the first color's unknowns (the L sweep
-// of color 0 is the identity, so its output is written here instead).
+// After step 1: rt = p = r.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_init_vectors(const Ctl *ctl, int n, int n0, const T *__restrict__ r, T *__restrict__ rt,
-               T *__restrict__ p, T *__restrict__ ph) {
+k_init_vectors(const Ctl *ctl, int n, const T *__restrict__ r, T *__restrict__ rt,
+               T *__restrict__ p) {
   if (ctl->done) return;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const T v = r[i];
     rt[i] = v;
     p[i] = v;
-    if (i < n0) ph[i] = v;
   }
 }
 
@@ -728,15 +726,13 @@ k_init_vectors(const Ctl *ctl, int n, int n0, const T *__restrict__ r, T *__rest
 // rho = ||rhs||^2 (step 1 without the SpMV of step 0).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_init_rhs(Ctl *ctl, int n, int n0, const T *__restrict__ rhs, T *__restrict__ r,
-           T *__restrict__ rt, T *__restrict__ p, T *__restrict__ ph, T *__restrict__ x,
-           double *partials) {
+k_init_rhs(Ctl *ctl, int n, const T *__restrict__ rhs, T *__restrict__ r,
+           T *__restrict__ rt, T *__restrict__ p, T *__restrict__ x, double *partials) {
   double d = 0.0;
   DF f = {0.f, 0.f};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const T v = rhs[i];
     r[i] = v; rt[i] = v; p[i] = v; x[i] = 0;
-    if (i < n0) ph[i] = v;
     if (sizeof(T) == 8) d += (double)v * v; else df_add_prod(f, (float)v, (float)v);
   }
   if (sizeof(T) == 4) d = df_value(f);
@@ -746,12 +742,11 @@ k_init_rhs(Ctl *ctl, int n, int n0, const T *__restrict__ rhs, T *__restrict__ r
 }
 
 // Steps 6-8 without the x update (deferred to the second half): s = r - alpha v,
-// ||s|| and the stop tests (solver.vhd:867-936, is_final_iter solver.vhd:557);
-// s^ = s on the first color's unknowns.
+// ||s|| and the stop tests (solver.vhd:867-936, is_final_iter solver.vhd:557).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_update_s(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
-           T *__restrict__ s, T *__restrict__ sh, double *partials) {
+k_update_s(Ctl *ctl, int n, const T *__restrict__ r, const T *__restrict__ v,
+           T *__restrict__ s, double *partials) {
   if (ctl->done) return;
   const T alpha = (T)ctl->alpha;
   double d = 0.0;
@@ -771,7 +766,6 @@ k_update_s(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict
       if (i < n) {
         const T si = fma(-alpha, vv4[u], rv[u]);
         s[i] = si;
-        if (i < n0) sh[i] = si;
         if (sizeof(T) == 8) d += (double)si * si; else df_add_prod(f, (float)si, (float)si);
       }
     }
@@ -861,16 +855,15 @@ k_update_r(Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph,
 // RESID, which set norm0 and the bound): the FP32 iteration works on
 // r64 / sigma with sigma = ||r64||; correction xc = 0.
 __global__ void __launch_bounds__(kThreads)
-k_ru_init(Ctl *ctl, int n, int n0, double delta, const double *__restrict__ r64,
+k_ru_init(Ctl *ctl, int n, double delta, const double *__restrict__ r64,
           float *__restrict__ r, float *__restrict__ rt, float *__restrict__ p,
-          float *__restrict__ ph, float *__restrict__ xc, double *partials) {
+          float *__restrict__ xc, double *partials) {
   if (ctl->done) return;
   const double inv = 1.0 / ctl->norm0;
   DF f = {0.f, 0.f};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const float v = (float)(r64[i] * inv);
     r[i] = v; rt[i] = v; p[i] = v; xc[i] = 0.f;
-    if (i < n0) ph[i] = v;
     df_add_prod(f, v, v);
   }
   double vv[1] = {df_value(f)}, tot[1];
@@ -930,12 +923,12 @@ k_ru_replace(Ctl *ctl, int n, const double *__restrict__ r64, float *__restrict_
   }
 }
 
-// Steps 15-17 (update_p, vector_ops.vhd:429-434): p = r + beta (p - omega v);
-// p^ = p on the first color's unknowns. Also drives the graph's while loop.
+// Steps 15-17 (update_p, vector_ops.vhd:429-434): p = r + beta (p - omega v).
+// Also drives the graph's while loop.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_update_p(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict__ v,
-           T *__restrict__ p, T *__restrict__ ph, unsigned long long cond) {
+k_update_p(Ctl *ctl, int n, const T *__restrict__ r, const T *__restrict__ v,
+           T *__restrict__ p, unsigned long long cond) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctl->body_runs += 1;
     // hard stop as a second guard: the loop can never run past maxit + 1
@@ -948,7 +941,6 @@ k_update_p(Ctl *ctl, int n, int n0, const T *__restrict__ r, const T *__restrict
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const T pi = fma(beta, fma(-omega, v[i], p[i]), r[i]);
     p[i] = pi;
-    if (i < n0) ph[i] = pi;
   }
 }
 

@@ -40,15 +40,34 @@ int orc_color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
   return ncolors;
 }
 
-void orc_color_order(int nb, const int *color, int ncolors, int *perm,
-                     int *color_ptr) {
+void orc_color_order(int nb, const int *rowptr, const int *colind,
+                     const int *color, int ncolors, int *perm, int *color_ptr,
+                     int *split) {
+  /* higher[i] = 1: row i shares a block with a row of a higher color */
+  char *higher = (char *)calloc((size_t)nb + 1, 1);
+  for (int i = 0; i < nb; ++i)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      int j = colind[k];
+      if (color[j] > color[i]) higher[i] = 1;
+      if (color[i] > color[j]) higher[j] = 1;
+    }
   for (int c = 0; c <= ncolors; ++c) color_ptr[c] = 0;
-  for (int i = 0; i < nb; ++i) color_ptr[color[i] + 1]++;
+  for (int c = 0; c < ncolors; ++c) split[c] = 0;
+  for (int i = 0; i < nb; ++i) {
+    color_ptr[color[i] + 1]++;
+    if (higher[i]) split[color[i]]++;
+  }
   for (int c = 0; c < ncolors; ++c) color_ptr[c + 1] += color_ptr[c];
-  int *fill = (int *)malloc(sizeof(int) * (size_t)(ncolors > 0 ? ncolors : 1));
-  for (int c = 0; c < ncolors; ++c) fill[c] = color_ptr[c];
-  for (int i = 0; i < nb; ++i) perm[fill[color[i]]++] = i;
-  free(fill);
+  int *first = (int *)malloc(sizeof(int) * (size_t)(ncolors > 0 ? ncolors : 1));
+  int *second = (int *)malloc(sizeof(int) * (size_t)(ncolors > 0 ? ncolors : 1));
+  for (int c = 0; c < ncolors; ++c) {
+    first[c] = color_ptr[c];
+    second[c] = color_ptr[c] + split[c];
+  }
+  for (int i = 0; i < nb; ++i) perm[higher[i] ? first[color[i]]++ : second[color[i]]++] = i;
+  free(first);
+  free(second);
+  free(higher);
 }
 
 void orc_permute_bsr(int nb, const int *rowptr, const int *colind,

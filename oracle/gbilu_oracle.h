@@ -42,10 +42,15 @@ enum {
  * neighbour. Returns the number of colors. */
 int orc_color_greedy(int nb, const int *rowptr, const int *colind, int *color);
 
-/* perm[new] = old: rows ordered by color, natural order inside a color.
- * color_ptr[c]..color_ptr[c+1] is the new-index range of color c. */
-void orc_color_order(int nb, const int *color, int ncolors, int *perm,
-                     int *color_ptr);
+/* perm[new] = old: rows ordered by color; inside a color, the rows that
+ * share a block with a row of a higher color (as either end) come first,
+ * then the others, each group in natural order. color_ptr[c]..color_ptr[c+1]
+ * is the new-index range of color c and split[c] the size of its first
+ * group. (The rows of one color are never coupled, so this order inside a
+ * color does not change the ILU0 factors.) */
+void orc_color_order(int nb, const int *rowptr, const int *colind,
+                     const int *color, int ncolors, int *perm, int *color_ptr,
+                     int *split);
 
 /* Permuted copy P A P^T with columns sorted inside each row.
  * prowptr[nb+1], pcolind[nnzb], pvals[nnzb*9]; src[k] = input block index. */

@@ -1,7 +1,8 @@
 """Regenerates the golden fixtures of the CPU oracle (tests/golden/*.npz).
 
 Each fixture stores a small seeded system (generator parameters and the
-generated arrays) with the oracle's outputs on it: coloring, permutation,
+generated arrays) with the oracle's outputs on it: coloring, permutation
+(with the split of each color),
 ILU0 factors, one SpMV and one ILU apply of a probe vector, and a solve
 (half-iteration count and solution). test_oracle.py checks that the oracle
 reproduces them bit for bit. The oracle is compiled with -ffp-contract=off
@@ -37,7 +38,7 @@ if __name__ == "__main__":
             os.path.join(HERE, name), grid=np.array(c["grid"]), sigma=c["sigma"],
             inactive=c["inactive"], faults=c["faults"], seed=c["seed"], tol=c["tol"],
             rowptr=s.rowptr, colind=s.colind, vals=s.vals.reshape(-1), b=s.b,
-            ncolors=P.ncolors, color=P.color, perm=P.perm, lu=P.lu, dinv=P.dinv,
+            ncolors=P.ncolors, color=P.color, perm=P.perm, split=P.split, lu=P.lu, dinv=P.dinv,
             x_probe=xp, spmv=P.spmv(xp), ilu=P.ilu_apply(xp), spmv_t=P.spmv(xp, True),
             ilu_t=P.ilu_apply(xp, True), half_iters=r.half_iters, x=x)
         print(name, s.nb, P.ncolors, r.half_iters)

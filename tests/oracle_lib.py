@@ -37,7 +37,8 @@ def lib():
         L = C.CDLL(ORACLE_SO)
         L.orc_color_greedy.argtypes = [C.c_int, I32P, I32P, I32P]
         L.orc_color_greedy.restype = C.c_int
-        L.orc_color_order.argtypes = [C.c_int, I32P, C.c_int, I32P, I32P]
+        L.orc_color_order.argtypes = [C.c_int, I32P, I32P, I32P, C.c_int, I32P, I32P,
+                                      I32P]
         L.orc_permute_bsr.argtypes = [C.c_int, I32P, I32P, F64P, I32P, I32P,
                                       I32P, F64P, I32P]
         L.orc_bilu0.argtypes = [C.c_int, I32P, I32P, F64P, F64P]
@@ -81,7 +82,9 @@ class Prepared:
         self.ncolors = L.orc_color_greedy(nb, rp, ci, self.color)
         self.perm = np.empty(nb, np.int32)
         self.color_ptr = np.empty(self.ncolors + 1, np.int32)
-        L.orc_color_order(nb, self.color, self.ncolors, self.perm, self.color_ptr)
+        self.split = np.empty(self.ncolors, np.int32)
+        L.orc_color_order(nb, rp, ci, self.color, self.ncolors, self.perm, self.color_ptr,
+                          self.split)
         self.iperm = np.empty(nb, np.int32)
         self.iperm[self.perm] = np.arange(nb, dtype=np.int32)
         nnzb = int(rp[-1])

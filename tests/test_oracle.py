@@ -51,6 +51,22 @@ def test_coloring_valid(prep):
     assert np.array_equal(np.sort(P.perm), np.arange(s.nb))
     assert np.all(np.diff(P.color[P.perm]) >= 0)
     assert P.color_ptr[-1] == s.nb
+    # inside each color: rows with a higher-colored neighbour (either end)
+    # first, then the others, each group in natural order
+    higher = np.zeros(s.nb, bool)
+    for i in range(s.nb):
+        for k in range(s.rowptr[i], s.rowptr[i + 1]):
+            j = s.colind[k]
+            if P.color[j] > P.color[i]:
+                higher[i] = True
+            elif P.color[j] < P.color[i]:
+                higher[j] = True
+    for c in range(P.ncolors):
+        rows = P.perm[P.color_ptr[c]:P.color_ptr[c + 1]]
+        sp_ = int(P.split[c])
+        assert np.all(higher[rows[:sp_]]) and not np.any(higher[rows[sp_:]])
+        assert np.all(np.diff(rows[:sp_]) > 0) and np.all(np.diff(rows[sp_:]) > 0)
+    assert P.split[-1] == 0
 
 
 def test_ilu_identity(prep):
@@ -185,6 +201,7 @@ def test_golden_fixtures(name):
     P = Prepared(s)
     assert P.ncolors == int(f["ncolors"])
     assert np.array_equal(P.color, f["color"]) and np.array_equal(P.perm, f["perm"])
+    assert np.array_equal(P.split, f["split"])
     assert np.array_equal(P.lu, f["lu"]) and np.array_equal(P.dinv, f["dinv"])
     x = f["x_probe"]
     assert np.array_equal(P.spmv(x), f["spmv"])
