@@ -299,8 +299,14 @@ enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3, 
 // omega = (y,w)/(y,y) (step 10). TRUE: y = b - A x and ||y|| into
 // Ctl::true_norm, only when a residual replacement is due.
 // V: matrix value type, T: vector type.
+// CTAs per SM the register budget must allow: the FP32 SpMV is HBM-bound
+// and gains from a third CTA (80 registers, no spills); the FP64 one is
+// bound by the FP64 pipe and keeps two
+#ifndef GBILU_SPMV32_MINB
+#define GBILU_SPMV32_MINB 3
+#endif
 template <typename V, typename T, int MODE>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, sizeof(V) == 4 ? GBILU_SPMV32_MINB : 2)
 k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
        T *__restrict__ y, const T *__restrict__ w, double *partials) {
@@ -938,9 +944,20 @@ k_update_p(Ctl *ctl, int n, const T *__restrict__ r, const T *__restrict__ v,
   }
   if (ctl->done) return;
   const T beta = (T)ctl->beta, omega = (T)ctl->omega;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const T pi = fma(beta, fma(-omega, v[i], p[i]), r[i]);
-    p[i] = pi;
+  const int stride = gridDim.x * kThreads;
+  // 4 elements per trip: their loads are in flight together
+  for (int i0 = blockIdx.x * kThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    T rv[4], vv4[4], pv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) { rv[u] = r[i]; vv4[u] = v[i]; pv[u] = p[i]; }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * stride;
+      if (i < n) p[i] = fma(beta, fma(-omega, vv4[u], pv[u]), rv[u]);
+    }
   }
 }
 
