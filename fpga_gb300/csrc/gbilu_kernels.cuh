@@ -944,20 +944,9 @@ k_update_p(Ctl *ctl, int n, const T *__restrict__ r, const T *__restrict__ v,
   }
   if (ctl->done) return;
   const T beta = (T)ctl->beta, omega = (T)ctl->omega;
-  const int stride = gridDim.x * kThreads;
-  // 4 elements per trip: their loads are in flight together
-  for (int i0 = blockIdx.x * kThreads + threadIdx.x; i0 < n; i0 += 4 * stride) {
-    T rv[4], vv4[4], pv[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u * stride;
-      if (i < n) { rv[u] = r[i]; vv4[u] = v[i]; pv[u] = p[i]; }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int i = i0 + u * stride;
-      if (i < n) p[i] = fma(beta, fma(-omega, vv4[u], pv[u]), rv[u]);
-    }
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const T pi = fma(beta, fma(-omega, v[i], p[i]), r[i]);
+    p[i] = pi;
   }
 }
 
