@@ -389,6 +389,24 @@ def mixed_adjoint_2m(local):
     return res
 
 
+def mixed_only(args):
+    """Mixed solves of the 500k-cell system to 1e-8, timed alone (profiler target)."""
+    from fpga_gb300 import GbIlu
+    from fpga_gb300.synth import make_config
+    s = make_config(WORKLOAD)
+    g = GbIlu(device=0, precision="mixed", use_graph=not args.no_graph)
+    g.analyze(s.rowptr, s.colind).factor(s.vals)
+    for _ in range(args.warmup):
+        g.solve(s.b, tol=1e-8, maxit=2000)
+    ms = []
+    for _ in range(args.steps):
+        x, r = g.solve(s.b, tol=1e-8, maxit=2000)
+        ms.append(r.device_ms)
+    print(json.dumps({"mixed_ms": statistics.median(ms), "outer": r.outer_iters,
+                      "inner_half_iters": r.inner_half_iters, "true_relres": r.true_relres}),
+          flush=True)
+
+
 def kernel_only(args):
     """One kernel family of the 500k-cell system timed alone (profiler target)."""
     from fpga_gb300 import GbIlu
@@ -415,7 +433,13 @@ def main():
     ap.add_argument("--kernel-only", default=None,
                     choices=["spmv64", "ilu64", "spmv32", "ilu32"],
                     help="time one kernel family alone (3 warm-up + --steps launches)")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="only mixed solves of the 500k-cell system to 1e-8 (profiler runs of "
+                         "the FP32 iteration kernels; combine with --no-graph)")
     args = ap.parse_args()
+    if args.mixed_only:
+        mixed_only(args)
+        return
     if args.kernel_only:
         kernel_only(args)
         return
