@@ -867,7 +867,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->device = 0;
   o->use_graph = 1;
   o->timeout_ms = 0.0;
-  o->inner_tol = 1e-2;
+  o->inner_tol = 1e-1;
   o->inner_maxit = 500;
   o->max_outer = 30;
   o->verbose = 0;

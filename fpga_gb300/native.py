@@ -125,7 +125,7 @@ class GbIlu:
     """
 
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
-                 timeout_ms=0.0, inner_tol=1e-2, inner_maxit=500, max_outer=30,
+                 timeout_ms=0.0, inner_tol=1e-1, inner_maxit=500, max_outer=30,
                  verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
                  ru_delta=0.1):
         self.L = load()

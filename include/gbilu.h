@@ -135,7 +135,7 @@ typedef struct {
 } gbilu_stats;
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
- * no timeout, inner_tol 1e-2, inner_maxit 500, max_outer 30, single-launch
+ * no timeout, inner_tol 1e-1, inner_maxit 500, max_outer 30, single-launch
  * sweeps, host factorization, mixed scheme 0, ru_delta 0.1 */
 int gbilu_default_options(gbilu_options *opt);
 
