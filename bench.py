@@ -4,7 +4,8 @@ Metric: ILU0-BiCGSTAB solve time on the 100x100x50 (500k-cell, 1.425M
 unknowns) system at relative residual 1e-2, FP64 (``value``, ms per solve,
 inputs resident in HBM), the same through the host-buffer C-ABI call
 (``e2e``), the mixed-precision form against FP64 at 1e-8 on the sigma=2.0
-system, and the adjoint/forward time ratio on the 60x60x30 system.
+system, the adjoint/forward time ratio on the 60x60x30 system, and the
+4,000-cell and 500k-cell systems at their tolerances in both forms.
 
 A "step" is one solve of the 500k-cell system from x0 = 0. Inputs are larger
 than L2 (the matrix values alone are 0.23 GB), so no L2 flush is inserted.
@@ -324,6 +325,29 @@ def secondary(args, local, tol64):
                     "mixed_outer": times["mixed"][1].outer_iters,
                     "mixed_inner_half_iters": times["mixed"][1].inner_half_iters,
                     "true_relres": tr, "x_err_vs_fp64": err}
+    # the 4,000-cell system at 1e-2 and the 500k-cell one at 1e-2 and 1e-6,
+    # FP64 and mixed
+    rows = []
+    for wl, tols in (("c1_20x20x10", (1e-2,)), (WORKLOAD, (1e-2, 1e-6))):
+        s2 = make_config(wl)
+        A2 = s2.to_scipy()
+        for prec in ("fp64", "mixed"):
+            g = GbIlu(device=local, precision=prec)
+            g.analyze(s2.rowptr, s2.colind).factor(s2.vals)
+            for tol2 in tols:
+                g.solve(s2.b, tol=tol2, maxit=CONFIGS[wl]["maxit"])
+                ms = []
+                for _ in range(3):
+                    x, r = g.solve(s2.b, tol=tol2, maxit=CONFIGS[wl]["maxit"])
+                    ms.append(r.device_ms)
+                rows.append({"workload": wl, "precision": prec, "tol": tol2,
+                             "ms": statistics.median(ms),
+                             "half_iters": r.half_iters if prec == "fp64" else r.inner_half_iters,
+                             "outer": r.outer_iters,
+                             "true_relres": float(np.linalg.norm(s2.b - A2 @ x) /
+                                                  np.linalg.norm(s2.b))})
+            g.close()
+    out["tolerances"] = rows
     # adjoint / forward on the 60x60x30 system
     c4 = CONFIGS["c4_60x60x30_adjoint"]
     s = make_config("c4_60x60x30_adjoint")
