@@ -1182,6 +1182,22 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   return GBILU_OK;
 }
 
+int gbilu_schedule(void *handle, int transpose, int cap, int *nsteps, int *steps) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  const PhaseList pl = make_phases(h->an, transpose != 0);
+  if (nsteps) *nsteps = pl.n;
+  for (int q = 0; q < pl.n && q < cap && steps; ++q) {
+    const Phase &P = pl.p[q];
+    // every step starts at a slice edge and ends with a grid barrier
+    const int v[13] = {P.row0, P.nrows, P.slice0, 0, P.mat, P.has_d, P.own_y, P.nbr_hat,
+                       P.src_rows, P.to_y, P.final0, P.final_d, 1};
+    memcpy(steps + 13 * q, v, sizeof v);
+  }
+  return GBILU_OK;
+}
+
 int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows, int cap,
                     int *nphases) {
   Handle *h = static_cast<Handle *>(handle);

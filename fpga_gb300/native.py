@@ -105,6 +105,7 @@ def load():
     L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
     L.gbilu_ilu_trace.argtypes = [VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_int)]
+    L.gbilu_schedule.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_int), VP]
     L.gbilu_status_string.argtypes = [C.c_int]
     L.gbilu_status_string.restype = C.c_char_p
     L.gbilu_last_error.argtypes = [VP]
@@ -261,6 +262,19 @@ class GbIlu:
         self._check(self.L.gbilu_ilu_trace(self.h, int(fp32), int(transpose), us.ctypes.data,
                                            rows.ctypes.data, 96, C.byref(n)))
         return [(int(rows[i]), float(us[i])) for i in range(n.value)]
+
+    SCHEDULE_FIELDS = ("row0", "nrows", "slice0", "lane0", "mat", "has_d", "own_y", "nbr_hat",
+                       "src_rows", "to_y", "final0", "final_d", "barrier_after")
+
+    def schedule(self, transpose=False):
+        """Steps of the single-launch ILU apply: a list of dicts (SCHEDULE_FIELDS)."""
+        n = C.c_int()
+        self._check(self.L.gbilu_schedule(self.h, int(transpose), 0, C.byref(n), None))
+        buf = np.zeros(13 * max(n.value, 1), np.int32)
+        self._check(self.L.gbilu_schedule(self.h, int(transpose), n.value, C.byref(n),
+                                          buf.ctypes.data))
+        return [dict(zip(self.SCHEDULE_FIELDS, map(int, buf[13 * q:13 * q + 13])))
+                for q in range(n.value)]
 
     def bench_kernel(self, which, reps=20):
         """(avg ms, algorithmic bytes, launches) per application of a kernel family."""

@@ -212,6 +212,16 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
  * step plus the grid barrier after it) and its row count. The GB300
  * counterpart of the reference's periodic debug lines (solver.vhd:1106-1133),
  * per color step instead of per sampling interval. */
+/* The step list of the single-launch ILU apply (forward or transposed) for
+ * the analyzed pattern, a diagnostic of its schedule: per step 13 ints
+ * {row0, nrows, slice0, lane0 (lane of row0 in its slice), matrix (0: first
+ * sweep, 1: second), has_d, own_y, nbr_hat, src_rows, to_y, final0,
+ * final_d, barrier_after (a grid barrier ends the step)}. Up to cap steps
+ * are written; *nsteps gets the count. Works on host-only handles.
+ * Counterpart of the reference's per-color processing order
+ * (sparstition.vhd:751-756, ilu0.vhd:293-323,406-417). */
+int gbilu_schedule(void *handle, int transpose, int cap, int *nsteps, int *steps);
+
 int gbilu_ilu_trace(void *handle, int fp32, int transpose, double *us, int *rows,
                     int cap, int *nphases);
 

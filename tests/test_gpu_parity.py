@@ -183,8 +183,8 @@ def test_ilu_trace(case):
     s, P, g = case
     for transpose in (False, True):
         tr = g.ilu_trace(transpose=transpose)
-        C = P.ncolors
-        assert len(tr) == (max(1, 2 * C - 2) if not transpose else 2 * C - 1)
+        steps = g.schedule(transpose)
+        assert len(tr) == len(steps) and [r for r, _ in tr] == [st["nrows"] for st in steps]
         assert sum(r for r, _ in tr) >= s.nb and all(us >= 0 for _, us in tr)
 
 

@@ -1,0 +1,96 @@
+"""The step schedule of the single-launch ILU apply (gbilu_schedule), checked
+on the CPU against the sparsity pattern: every value a step reads was written
+in an earlier barrier interval (steps that share an interval are
+independent), every z row is written exactly once, every y row at most once.
+Runs on host-only handles (no GPU)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from fpga_gb300 import GbIlu
+from fpga_gb300.synth import generate, make_config
+
+CASES = {
+    "c1": lambda: make_config("c1_20x20x10"),
+    "faults": lambda: generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7),
+    "mid": lambda: generate(60, 60, 20, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=5),
+    "sigma2": lambda: generate(40, 40, 16, sigma=2.0, inactive_frac=0.05, fault_frac=0.02, seed=3),
+}
+
+
+def permuted_pattern(s, perm):
+    nb = s.nb
+    iperm = np.empty(nb, np.int64)
+    iperm[perm] = np.arange(nb)
+    A = sp.csr_matrix((np.ones(len(s.colind)), s.colind, s.rowptr), shape=(nb, nb))
+    P = A[perm][:, perm].tocsr()
+    P.sort_indices()
+    return P
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("transpose", [False, True])
+def test_schedule_dependencies(built_lib, name, transpose):
+    s = CASES[name]()
+    g = GbIlu(device=-1)
+    g.analyze(s.rowptr, s.colind)
+    _, _, perm, _ = g.ordering()
+    P = permuted_pattern(s, perm)
+    low, up = sp.tril(P, -1).tocsr(), sp.triu(P, 1).tocsr()
+    if transpose:   # U^T and L^T rows: the pattern's columns, transposed
+        first, second = up.T.tocsr(), low.T.tocsr()
+    else:
+        first, second = low, up
+    nb = s.nb
+    wy = np.full(nb, -1)
+    wh = np.full(nb, -1)
+    steps = g.schedule(transpose)
+    assert steps and steps[-1]["barrier_after"] in (0, 1)
+    k = 0
+    pend_y, pend_h = [], []
+    for st in steps:
+        rows = np.arange(st["row0"], st["row0"] + st["nrows"])
+        M = second if st["mat"] else first
+        sub = M[rows]
+        cols = sub.indices
+        # own values
+        if st["own_y"]:
+            assert np.all((wy[rows] >= 0) & (wy[rows] < k)), "own y not ready"
+        # neighbours
+        from_src = cols < st["src_rows"]
+        c = cols[~from_src]
+        w = wh[c] if st["nbr_hat"] else wy[c]
+        assert np.all((w >= 0) & (w < k)), "neighbour not ready"
+        # writes
+        if st["to_y"]:
+            pend_y.append(rows)
+            fin = rows[rows >= st["final0"]]
+            pend_h.append(fin)
+        else:
+            pend_h.append(rows)
+        if st["barrier_after"]:
+            for r in pend_y:
+                assert np.all(wy[r] == -1), "y written twice"
+                wy[r] = k
+            for r in pend_h:
+                assert np.all(wh[r] == -1), "z written twice"
+                wh[r] = k
+            pend_y, pend_h = [], []
+            k += 1
+    for r in pend_y:
+        assert np.all(wy[r] == -1)
+        wy[r] = k
+    for r in pend_h:
+        assert np.all(wh[r] == -1)
+        wh[r] = k
+    assert np.all(wh >= 0), "rows without a final value"
+    # slice0 / lane0 agree with the layout: a color's slices hold 32
+    # consecutive rows from the color's first row on
+    _, _, _, cp = g.ordering()
+    base = {}
+    for st in steps:
+        assert 0 <= st["lane0"] < 32
+        c = int(np.searchsorted(cp, st["row0"], side="right") - 1)
+        off = st["slice0"] * 32 + st["lane0"] - st["row0"]
+        assert base.setdefault(c, off) == off
+        assert (st["row0"] - cp[c]) % 32 == st["lane0"]
