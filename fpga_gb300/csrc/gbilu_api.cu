@@ -699,7 +699,10 @@ int check_solve_ready(Handle *h) {
 }
 
 // FP64 BiCGSTAB on the permuted vectors: b in h->b64, x in v64.x.
-int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long long &launches) {
+// With sync false the final Ctl is only queued for copy into h->h_ctl: the
+// caller synchronizes once at the end (no host round trip mid-solve).
+int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long long &launches,
+            bool sync = true) {
   const int n = 3 * h->an.nb;
   Ops<double, double> o = make_ops<double, double>(h, transpose);
   Vecs<double> &w = h->v64;
@@ -714,6 +717,7 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   int rc = run_loop<double, double>(h, transpose, maxit, launches);
   if (rc) return rc;
   CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+  if (!sync) return GBILU_OK;
   CK(cudaStreamSynchronize(h->st));
   out = *h->h_ctl;
   if (h->opt.use_graph) launches += (long long)out.body_runs * h->per_iter[transpose ? 1 : 0];
@@ -1029,21 +1033,28 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   memset(&tmp, 0, sizeof tmp);
   gbilu_result *r = res ? res : &tmp;
   memset(r, 0, sizeof *r);
-  if (h->opt.precision == GBILU_MIXED)
+  const bool fp64 = h->opt.precision != GBILU_MIXED;
+  if (!fp64)
     rc = solve_mixed(h, transpose, tol, maxit, r, c, launches);
   else
-    rc = solve64(h, transpose, tol, maxit, c, launches);
+    rc = solve64(h, transpose, tol, maxit, c, launches, false);
   if (rc) return rc;
+  // x back to the caller's numbering. When the initial residual already met
+  // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged
+  // bit for bit; the FP64 path therefore needs no status before it and the
+  // whole solve ends in one host synchronization.
   double *out = device_ptrs ? x : h->io64b.p;
-  if (c.status != ST_ALREADY) {
-    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p, out);
-    launches += 1;
-  }
+  k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p, out);
+  launches += 1;
   CK(cudaEventRecord(h->e1, h->st));
-  if (!device_ptrs && c.status != ST_ALREADY)
+  if (!device_ptrs)
     CK(cudaMemcpyAsync(x, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   CK(last_error(h));
+  if (fp64) {
+    c = *h->h_ctl;
+    if (h->opt.use_graph) launches += (long long)c.body_runs * h->per_iter[transpose ? 1 : 0];
+  }
   const int outer = r->outer_iters, inner = r->inner_half_iters;
   const double tr = r->true_relres;
   fill_result(h, c, r);
