@@ -83,7 +83,7 @@ struct Handle {
   cudaStream_t st = nullptr, cap = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   DevBuf<int2> srows;
-  DevBuf<int> perm, prowptr, pcol, psrc;
+  DevBuf<int> perm, iperm, prowptr, pcol, psrc;
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
   DevBuf<float> dinv32, dinvT32;
@@ -553,7 +553,7 @@ void release_device(Handle *h) {
     }
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
-  h->srows.release(); h->perm.release(); h->prowptr.release(); h->pcol.release();
+  h->srows.release(); h->perm.release(); h->iperm.release(); h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
   h->io64.release(); h->io64b.release(); h->partials.release(); h->dA.release();
@@ -585,6 +585,8 @@ int setup_device(Handle *h) {
   CK(cudaMemcpy(h->srows.p, sr.data(), sr.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CK(h->perm.alloc(an.nb));
   CK(cudaMemcpy(h->perm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->iperm.alloc(an.nb));
+  CK(cudaMemcpy(h->iperm.p, an.iperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->prowptr.alloc(an.nb + 1));
   CK(cudaMemcpy(h->prowptr.p, an.prowptr.data(), (an.nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->pcol.alloc(an.nnzb));
@@ -635,7 +637,7 @@ int setup_device(Handle *h) {
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
-                     (size_t)an.nnzb * 8 + (size_t)an.nb * 8;
+                     (size_t)an.nnzb * 8 + (size_t)an.nb * 12;
   return GBILU_OK;
 }
 
@@ -1019,14 +1021,35 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   CK(cudaEventRecord(h->e0, h->st));
   const double *db = b;
   const double *dx = x;
+  double *mapped_x = nullptr;
   if (!device_ptrs) {
-    CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    db = h->io64.p;
-    dx = h->io64b.p;
+    // Page-locked host buffers are read and written by the gather/scatter
+    // kernels in place (mapped, over the CPU-GPU link); other host memory
+    // goes through staging copies.
+    cudaPointerAttributes ab, ax;
+    const bool zb = cudaPointerGetAttributes(&ab, b) == cudaSuccess &&
+                    ab.type == cudaMemoryTypeHost && ab.devicePointer;
+    const bool zx = cudaPointerGetAttributes(&ax, x) == cudaSuccess &&
+                    ax.type == cudaMemoryTypeHost && ax.devicePointer;
+    cudaGetLastError();   // a query on unregistered memory is not an error here
+    if (zb && zx) {
+      db = static_cast<const double *>(ab.devicePointer);
+      dx = mapped_x = static_cast<double *>(ax.devicePointer);
+    } else {
+      CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      db = h->io64.p;
+      dx = h->io64b.p;
+    }
   }
-  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, db, h->b64.p, 1.0);
-  k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
+  if (mapped_x) {
+    // host side read in order, device side written permuted
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, db, h->b64.p);
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, dx, h->v64.x.p);
+  } else {
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, db, h->b64.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
+  }
   launches += 2;
   Ctl c;
   gbilu_result tmp;
@@ -1043,11 +1066,14 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged
   // bit for bit; the FP64 path therefore needs no status before it and the
   // whole solve ends in one host synchronization.
-  double *out = device_ptrs ? x : h->io64b.p;
-  k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p, out);
+  if (mapped_x)   // device side read permuted, host side written in order
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, h->v64.x.p, mapped_x, 1.0);
+  else
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p,
+                                                 device_ptrs ? x : h->io64b.p);
   launches += 1;
   CK(cudaEventRecord(h->e1, h->st));
-  if (!device_ptrs)
+  if (!device_ptrs && !mapped_x)
     CK(cudaMemcpyAsync(x, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   CK(last_error(h));
