@@ -226,13 +226,13 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
 template <typename V, typename T>
 int coop_grid(Handle *h) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kCoopThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, coop_threads<T>(), 0);
   long long most = 0;
   for (int c = 0; c < h->an.ncolors; ++c) {
     const long long rows = h->an.color_ptr[c + 1] - h->an.color_ptr[c];
     most = std::max(most, rows);
   }
-  const int need = (int)((most + kCoopThreads - 1) / kCoopThreads);
+  const int need = (int)((most + coop_threads<T>() - 1) / coop_threads<T>());
   return std::max(1, std::min(per_sm * h->sm_count, need));
 }
 
@@ -289,7 +289,7 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
   CK(cudaMemcpy(h->stage_cnt[f][t].p, cnt.data(), cnt.size() * sizeof(int2), cudaMemcpyHostToDevice));
   CK(cudaFuncSetAttribute(k_ilu_coop<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBudget));
   int per_sm = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, kCoopThreads, (size_t)most));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, coop_threads<T>(), (size_t)most));
   if (per_sm < 1) {
     for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
     return GBILU_OK;
@@ -311,7 +311,7 @@ cudaError_t launch_coop(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.gridDim = dim3(f ? h->coop_grid32 : h->coop_grid64);
-  cfg.blockDim = dim3(kCoopThreads);
+  cfg.blockDim = dim3(coop_threads<T>());
   cfg.dynamicSmemBytes = (size_t)h->stage_bytes[f][t];
   cfg.stream = s;
   cfg.attrs = attr;

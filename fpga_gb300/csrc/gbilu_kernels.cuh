@@ -232,6 +232,10 @@ __device__ __forceinline__ void finish_init(Ctl *c, double rr) {
 #define GBILU_BATCH 4
 #endif
 constexpr int kBatch = GBILU_BATCH;   // blocks whose loads are in flight together
+#ifndef GBILU_BATCH64
+#define GBILU_BATCH64 2
+#endif
+constexpr int kBatch64 = GBILU_BATCH64;   // the same for FP64 values
 
 // Loads of vectors that other CTAs of the same kernel wrote go through L2
 // (ld.global.cg): the per-SM L1 is not coherent inside one launch.
@@ -252,7 +256,7 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
                                            int lo, T &a0, T &a1, T &a2) {
   // FP64 batches of 2 keep the kernels within 128 registers (the FP64 pipe,
   // not the load latency, bounds them); FP32 batches of kBatch
-  constexpr int B = sizeof(V) == 8 ? (kBatch < 2 ? kBatch : 2) : kBatch;
+  constexpr int B = sizeof(V) == 8 ? kBatch64 : kBatch;
   for (int k0 = 0; k0 < wdt; k0 += B) {
     int c[B];
 #pragma unroll
@@ -524,6 +528,16 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 #define GBILU_COOP_THREADS 512
 #endif
 constexpr int kCoopThreads = GBILU_COOP_THREADS;   // one CTA per SM: half the barrier arrivals
+// threads per CTA of the single-launch apply by vector precision
+#ifndef GBILU_COOP_THREADS64
+#define GBILU_COOP_THREADS64 GBILU_COOP_THREADS
+#endif
+#ifndef GBILU_COOP_THREADS32
+#define GBILU_COOP_THREADS32 GBILU_COOP_THREADS
+#endif
+template <typename T> __host__ __device__ constexpr int coop_threads() {
+  return sizeof(T) == 4 ? GBILU_COOP_THREADS32 : GBILU_COOP_THREADS64;
+}
 
 // Every spin is bounded: a barrier that does not complete within this many
 // polls marks the run failed (Ctl::bar_fail) and the kernel returns.
@@ -617,7 +631,7 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
 // L2 because earlier steps of the same launch wrote them on other SMs.
 // Staged small steps read their matrix data from shared memory.
 template <typename V, typename T>
-__global__ void __launch_bounds__(kCoopThreads, 1)
+__global__ void __launch_bounds__(coop_threads<T>(), 1)
 k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
            const int *__restrict__ col1, const V *__restrict__ val1, const int *__restrict__ off2,
            const int *__restrict__ col2, const V *__restrict__ val2, const V *__restrict__ dmat,
@@ -653,7 +667,8 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         bulk_g2s(dst + vb + cb, dmat + (size_t)s * 9 * 32, (uint32_t)(9 * 32 * sizeof(V)), &stage_bar);
     }
   }
-  const int stride = gridDim.x * kCoopThreads;
+  constexpr int NT = coop_threads<T>();
+  const int stride = gridDim.x * NT;
   for (int q = 0; q < ph.n; ++q) {
     if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
     const Phase P = ph.p[q];
@@ -679,7 +694,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         staged_ready = true;
       }
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int e = warp; e < stage_n; e += kCoopThreads / 32) {
+      for (int e = warp; e < stage_n; e += NT / 32) {
         const StageEntry E = stage_tab[e];
         if (E.q != q) continue;
         const int r = 32 * E.j + lane;
@@ -691,7 +706,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
       }
     } else {
-      for (int t = blockIdx.x * kCoopThreads + threadIdx.x; t < P.nrows; t += stride)
+      for (int t = blockIdx.x * NT + threadIdx.x; t < P.nrows; t += stride)
         phase_row<V, T, true>(P, P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
                               src, ybuf, hat);
     }
