@@ -89,23 +89,24 @@ __device__ __forceinline__ void df_add_prod(DF &acc, float a, float b) {
 }
 __device__ __forceinline__ double df_value(const DF &a) { return (double)a.hi + (double)a.lo; }
 
-// Deterministic block reduction of NV doubles; result valid in thread 0.
+// Deterministic block reduction of NV doubles over a kThreads-thread CTA;
+// result valid in thread 0. GB300's FP64 pipe is 1/64 of FP32, so a shuffle
+// tree in every warp (45 FP64 warp instructions per CTA) costs microseconds:
+// the values go through shared memory instead and warp 0 alone sums them, 8
+// per lane in order and then a 5-level shuffle tree (12 instructions).
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV]) {
-  __shared__ double red[NV][kWarps];
+  __shared__ double red[NV][kThreads];
 #pragma unroll
-  for (int j = 0; j < NV; ++j)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0)
-#pragma unroll
-    for (int j = 0; j < NV; ++j) red[j][w] = v[j];
+  for (int j = 0; j < NV; ++j) red[j][threadIdx.x] = v[j];
   __syncthreads();
-  if (w == 0) {
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
 #pragma unroll
     for (int j = 0; j < NV; ++j) {
-      double x = l < kWarps ? red[j][l] : 0.0;
+      double x = red[j][l];
+#pragma unroll
+      for (int k = 1; k < kWarps; ++k) x += red[j][l + 32 * k];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
       v[j] = x;
