@@ -83,7 +83,10 @@ struct Handle {
   cudaStream_t st = nullptr, cap = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   DevBuf<int2> srows;
-  DevBuf<int> perm, iperm, prowptr, pcol, psrc;
+  // perm/iperm: device row <-> input row (the vectors of a solve);
+  // fperm: permuted row -> input row (the pattern-ordered gradient);
+  // dperm: device row -> permuted row (the device factorization's layout)
+  DevBuf<int> perm, iperm, fperm, dperm, prowptr, pcol, psrc;
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
   DevBuf<float> dinv32, dinvT32;
@@ -553,7 +556,8 @@ void release_device(Handle *h) {
     }
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
-  h->srows.release(); h->perm.release(); h->iperm.release(); h->prowptr.release(); h->pcol.release();
+  h->srows.release(); h->perm.release(); h->iperm.release(); h->fperm.release(); h->dperm.release();
+  h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
   h->io64.release(); h->io64b.release(); h->partials.release(); h->dA.release();
@@ -583,10 +587,21 @@ int setup_device(Handle *h) {
   for (int s = 0; s < an.S; ++s) sr[s] = make_int2(an.slice_row0[s], an.slice_len[s]);
   CK(h->srows.alloc(an.S));
   CK(cudaMemcpy(h->srows.p, sr.data(), sr.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  CK(h->perm.alloc(an.nb));
-  CK(cudaMemcpy(h->perm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
-  CK(h->iperm.alloc(an.nb));
-  CK(cudaMemcpy(h->iperm.p, an.iperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> dv(an.nb), idv(an.nb);
+    for (int d = 0; d < an.nb; ++d) {
+      dv[d] = an.perm[an.dperm[d]];
+      idv[dv[d]] = d;
+    }
+    CK(h->perm.alloc(an.nb));
+    CK(cudaMemcpy(h->perm.p, dv.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+    CK(h->iperm.alloc(an.nb));
+    CK(cudaMemcpy(h->iperm.p, idv.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  CK(h->fperm.alloc(an.nb));
+  CK(cudaMemcpy(h->fperm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->dperm.alloc(an.nb));
+  CK(cudaMemcpy(h->dperm.p, an.dperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->prowptr.alloc(an.nb + 1));
   CK(cudaMemcpy(h->prowptr.p, an.prowptr.data(), (an.nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->pcol.alloc(an.nnzb));
@@ -637,7 +652,7 @@ int setup_device(Handle *h) {
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
-                     (size_t)an.nnzb * 8 + (size_t)an.nb * 12;
+                     (size_t)an.nnzb * 8 + (size_t)an.nb * 20;
   return GBILU_OK;
 }
 
@@ -681,11 +696,11 @@ int factor_device(Handle *h, const double *vals) {
   fill_mat_device(h, h->Lt, h->pbuf.p);
   fill_mat_device(h, h->Ut, h->pbuf.p);
   const int gd = grid_for(h, (long long)an.S * 32);
-  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 0, h->dinvp.p, h->dinv64.p);
-  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 1, h->dinvp.p, h->dinvT64.p);
+  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, h->dperm.p, 0, h->dinvp.p, h->dinv64.p);
+  k_fill_diag<double><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, h->dperm.p, 1, h->dinvp.p, h->dinvT64.p);
   if (h->with_32) {
-    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 0, h->dinvp.p, h->dinv32.p);
-    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, 1, h->dinvp.p, h->dinvT32.p);
+    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, h->dperm.p, 0, h->dinvp.p, h->dinv32.p);
+    k_fill_diag<float><<<gd, kThreads, 0, h->st>>>(an.S, h->srows.p, h->dperm.p, 1, h->dinvp.p, h->dinvT32.p);
   }
   CK(cudaStreamSynchronize(h->st));
   CK(last_error(h));
@@ -1170,11 +1185,11 @@ int gbilu_adjoint(void *handle, const double *g_in, const double *x, double *lam
   if (dA) {
     const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
     CK(h->dA.n == (size_t)h->an.nnzb * 9 ? cudaSuccess : (h->dA.release(), h->dA.alloc((size_t)h->an.nnzb * 9)));
-    // lambda and x in the permuted numbering
+    // lambda and x in the permuted numbering (that of the pattern arrays)
     CK(cudaMemcpyAsync(h->io64.p, lambda, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64.p, h->v64.r.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, h->io64.p, h->v64.r.p, 1.0);
     CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->io64b.p, h->v64.s.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, h->io64b.p, h->v64.s.p, 1.0);
     k_grad_a<<<grid_for(h, nb), kThreads, 0, h->st>>>(nb, h->prowptr.p, h->pcol.p, h->psrc.p,
                                                       h->v64.r.p, h->v64.s.p, h->dA.p);
     CK(cudaMemcpyAsync(dA, h->dA.p, (size_t)h->an.nnzb * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -1216,6 +1231,14 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
     const double vec = 17.0 * n * sx;
     s->alg_bytes_iter[p] = 2 * s->alg_bytes_spmv[p] + 2 * s->alg_bytes_ilu[p] + vec;
   }
+  return GBILU_OK;
+}
+
+int gbilu_device_order(void *handle, int *order) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h || !order) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  for (int d = 0; d < h->an.nb; ++d) order[d] = h->an.perm[h->an.dperm[d]];
   return GBILU_OK;
 }
 

@@ -54,7 +54,10 @@ struct Csr {
   std::vector<int> rowptr, col, src;
 };
 
-// Builds the sliced layout of a CSR matrix (rows in permuted numbering).
+// Builds the sliced layout of a CSR matrix given in the permuted numbering:
+// lane l of slice s holds device row slice_row0[s] + l, i.e. permuted row
+// dperm[...], with its blocks in their CSR order and columns renumbered to
+// device rows.
 void slice_matrix(const Analysis &an, const Csr &m, bool transpose_blocks,
                   SlicedMatrix &out) {
   out.transpose_blocks = transpose_blocks;
@@ -62,7 +65,7 @@ void slice_matrix(const Analysis &an, const Csr &m, bool transpose_blocks,
   for (int s = 0; s < an.S; ++s) {
     int w = 0;
     for (int l = 0; l < an.slice_len[s]; ++l) {
-      const int r = an.slice_row0[s] + l;
+      const int r = an.dperm[an.slice_row0[s] + l];
       w = std::max(w, m.rowptr[r + 1] - m.rowptr[r]);
     }
     out.off[s + 1] = out.off[s] + w;
@@ -72,10 +75,10 @@ void slice_matrix(const Analysis &an, const Csr &m, bool transpose_blocks,
   out.vsrc.assign(n, -1);
   for (int s = 0; s < an.S; ++s) {
     for (int l = 0; l < an.slice_len[s]; ++l) {
-      const int r = an.slice_row0[s] + l;
+      const int r = an.dperm[an.slice_row0[s] + l];
       for (int k = m.rowptr[r]; k < m.rowptr[r + 1]; ++k) {
         const size_t slot = static_cast<size_t>(out.off[s]) + (k - m.rowptr[r]);
-        out.col[slot * kSliceRows + l] = m.col[k];
+        out.col[slot * kSliceRows + l] = an.idperm[m.col[k]];
         out.vsrc[slot * kSliceRows + l] = m.src[k];
       }
     }
@@ -201,6 +204,21 @@ std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
   }
   an.S = an.slice_color_ptr[C];
 
+  // device numbering: each color's split run and its other run, rows by
+  // descending block count (stable)
+  an.dperm.resize(nb);
+  an.idperm.resize(nb);
+  std::iota(an.dperm.begin(), an.dperm.end(), 0);
+  for (int c = 0; c < C; ++c) {
+    const int bounds[3] = {an.color_ptr[c], an.color_ptr[c] + an.split[c], an.color_ptr[c + 1]};
+    for (int g = 0; g < 2; ++g)
+      std::stable_sort(an.dperm.begin() + bounds[g], an.dperm.begin() + bounds[g + 1],
+                       [&](int x, int y) {
+                         return an.prowptr[x + 1] - an.prowptr[x] > an.prowptr[y + 1] - an.prowptr[y];
+                       });
+  }
+  for (int d = 0; d < nb; ++d) an.idperm[an.dperm[d]] = d;
+
   slice_matrix(an, a, false, an.A);
   slice_matrix(an, l, false, an.L);
   slice_matrix(an, u, false, an.U);
@@ -298,7 +316,7 @@ template <typename V>
 void fill_sliced_diag(const Analysis &an, const double *d, bool transpose, V *out) {
   for (int s = 0; s < an.S; ++s)
     for (int l = 0; l < kSliceRows; ++l) {
-      const int r = an.slice_row0[s] + l;
+      const int r = l < an.slice_len[s] ? an.dperm[an.slice_row0[s] + l] : 0;
       for (int e = 0; e < 9; ++e) {
         double x = 0.0;
         if (l < an.slice_len[s]) {

@@ -17,11 +17,12 @@ namespace gbilu {
 constexpr int kSliceRows = 32;  // block rows per slice = one warp
 
 // One matrix (A, L, U or a transpose) in the sliced layout shared by all
-// matrices of a handle. Slice s covers block rows slice_row0[s] ..
+// matrices of a handle. Slice s covers device rows slice_row0[s] ..
 // slice_row0[s] + slice_len[s] - 1 of one color; row lane l of slice s keeps
-// its k-th block in slot off[s] + k: column col[slot*32 + l] (-1 = padding,
-// always after the row's last block) and value entry e at
-// val[(slot*9 + e)*32 + l]. Blocks of a row are in ascending column order.
+// its k-th block in slot off[s] + k: column col[slot*32 + l] (a device row;
+// -1 = padding, always after the row's last block) and value entry e at
+// val[(slot*9 + e)*32 + l]. Blocks of a row are in ascending column order of
+// the permuted numbering.
 struct SlicedMatrix {
   std::vector<int> off;   // [S+1]
   std::vector<int> col;   // [slots*32]
@@ -41,6 +42,15 @@ struct Analysis {
   std::vector<int> prowptr, pcolind;      // permuted pattern, sorted columns
   std::vector<int> psrc;                  // permuted block -> input block
   std::vector<int> pdiag;                 // position of the diagonal block
+  // Device numbering: inside each run of a color's split rows and of its
+  // other rows, the rows by descending block count (stable), so that the 32
+  // rows of a slice have nearly equal widths and a slice carries almost no
+  // padding slots (a padded slot still costs the warp its FMA
+  // instructions). dperm[device row] = permuted row; idperm is its inverse.
+  // Only the sliced layouts and the device vectors use this numbering: the
+  // factorization, the factors and every row's block order stay those of
+  // the permuted numbering, so each row's arithmetic is unchanged.
+  std::vector<int> dperm, idperm;
   int nnzb_l = 0, nnzb_u = 0;
   // slices
   int S = 0;
@@ -75,7 +85,7 @@ template <typename V>
 void fill_sliced(const SlicedMatrix &m, const double *src, V *out);
 
 // Sliced copy of per-row 3x3 blocks (nb*9 doubles in permuted row order),
-// optionally transposed, laid out [(slice*9 + e)*32 + lane].
+// optionally transposed, laid out [(slice*9 + e)*32 + lane] by device row.
 template <typename V>
 void fill_sliced_diag(const Analysis &an, const double *dinv, bool transpose,
                       V *out);

@@ -707,9 +707,16 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
       }
     } else {
-      for (int t = blockIdx.x * NT + threadIdx.x; t < P.nrows; t += stride)
-        phase_row<V, T, true>(P, P.row0 + t, P.slice0 + (t >> 5), t & 31, off, col, val, dmat,
-                              src, ybuf, hat);
+      // slice j of the step goes to CTA j % grid: the device numbering puts
+      // a color's widest rows first, and contiguous chunks per CTA would
+      // hand them all to the first CTAs, which every barrier then waits for
+      const int lane = threadIdx.x & 31, nsl = (P.nrows + 31) >> 5;
+      for (int j = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; j < nsl; j += stride >> 5) {
+        const int t = 32 * j + lane;
+        if (t < P.nrows)
+          phase_row<V, T, true>(P, P.row0 + t, P.slice0 + j, lane, off, col, val, dmat, src, ybuf,
+                                hat);
+      }
     }
     bool ok = true;
     if (q + 1 < ph.n) ok = grid_barrier(ctl);
@@ -1158,10 +1165,11 @@ __global__ void k_fill_sliced(long long slots, const int *__restrict__ vsrc, int
   }
 }
 
-// Sliced per-row 3x3 blocks [(s*9 + e)*32 + lane] from nb*9 doubles.
+// Sliced per-row 3x3 blocks [(s*9 + e)*32 + lane] from nb*9 doubles in
+// permuted row order (drow: device row -> permuted row).
 template <typename V>
-__global__ void k_fill_diag(int S, const int2 *__restrict__ srows, int transpose,
-                            const double *__restrict__ d, V *__restrict__ out) {
+__global__ void k_fill_diag(int S, const int2 *__restrict__ srows, const int *__restrict__ drow,
+                            int transpose, const double *__restrict__ d, V *__restrict__ out) {
   for (long long q = blockIdx.x * (long long)kThreads + threadIdx.x; q < (long long)S * 32;
        q += (long long)gridDim.x * kThreads) {
     const int s = (int)(q >> 5), lane = (int)(q & 31);
@@ -1169,7 +1177,7 @@ __global__ void k_fill_diag(int S, const int2 *__restrict__ srows, int transpose
 #pragma unroll
     for (int e = 0; e < 9; ++e) {
       const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
-      const double x = lane < sr.y ? d[(size_t)(sr.x + lane) * 9 + ee] : 0.0;
+      const double x = lane < sr.y ? d[(size_t)drow[sr.x + lane] * 9 + ee] : 0.0;
       out[((size_t)s * 9 + e) * 32 + lane] = (V)x;
     }
   }

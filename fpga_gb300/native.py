@@ -93,6 +93,7 @@ def load():
     L.gbilu_destroy.argtypes = [VP]
     L.gbilu_analyze.argtypes = [VP, C.c_int, I32P, I32P]
     L.gbilu_get_ordering.argtypes = [VP, C.POINTER(C.c_int), VP, VP, VP]
+    L.gbilu_device_order.argtypes = [VP, VP]
     L.gbilu_factor.argtypes = [VP, F64P]
     L.gbilu_get_factors.argtypes = [VP, VP, VP]
     L.gbilu_solve.argtypes = [VP, VP, VP, C.c_double, C.c_int, C.POINTER(Result)]
@@ -198,6 +199,13 @@ class GbIlu:
         self._check(self.L.gbilu_get_ordering(self.h, C.byref(nc), color.ctypes.data,
                                               perm.ctypes.data, cp.ctypes.data))
         return nc.value, color, perm, cp
+
+    def device_order(self):
+        """Input row held at each device row (the numbering of the device
+        vectors and sliced layouts)."""
+        order = np.empty(self.nb, np.int32)
+        self._check(self.L.gbilu_device_order(self.h, order.ctypes.data))
+        return order
 
     def factors(self):
         lu = np.empty(9 * self.nnzb)

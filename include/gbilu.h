@@ -154,6 +154,16 @@ int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind);
 int gbilu_get_ordering(void *handle, int *ncolors, int *color, int *perm,
                        int *color_ptr);
 
+/* The numbering of the device vectors and sliced layouts: order[d] = input
+ * row held at device row d. It keeps perm's color ranges and each color's
+ * leading rows with a higher-colored neighbour, and inside each of these
+ * runs sorts the rows by descending block count so that the 32 rows of a
+ * slice carry nearly equal numbers of blocks (no padding slots). Row
+ * results are unchanged by it: every row keeps its blocks in the order of
+ * the permuted numbering. A diagnostic; the solve functions take and return
+ * vectors in input order. */
+int gbilu_device_order(void *handle, int *order);
+
 /* Block ILU0 of A (values in the order of the analyzed colind, nnzb*9
  * doubles) in the color-permuted order, FP64 3x3 inversions, and upload of
  * A, L, U and the inverted diagonal blocks to the device (the arrays

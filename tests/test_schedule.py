@@ -20,8 +20,6 @@ CASES = {
 
 def permuted_pattern(s, perm):
     nb = s.nb
-    iperm = np.empty(nb, np.int64)
-    iperm[perm] = np.arange(nb)
     A = sp.csr_matrix((np.ones(len(s.colind)), s.colind, s.rowptr), shape=(nb, nb))
     P = A[perm][:, perm].tocsr()
     P.sort_indices()
@@ -34,8 +32,7 @@ def test_schedule_dependencies(built_lib, name, transpose):
     s = CASES[name]()
     g = GbIlu(device=-1)
     g.analyze(s.rowptr, s.colind)
-    _, _, perm, _ = g.ordering()
-    P = permuted_pattern(s, perm)
+    P = permuted_pattern(s, g.device_order())   # the numbering the steps use
     low, up = sp.tril(P, -1).tocsr(), sp.triu(P, 1).tocsr()
     if transpose:   # U^T and L^T rows: the pattern's columns, transposed
         first, second = up.T.tocsr(), low.T.tocsr()
@@ -94,3 +91,34 @@ def test_schedule_dependencies(built_lib, name, transpose):
         off = st["slice0"] * 32 + st["lane0"] - st["row0"]
         assert base.setdefault(c, off) == off
         assert (st["row0"] - cp[c]) % 32 == st["lane0"]
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_device_order(built_lib, name):
+    """The device numbering permutes rows only inside each color's run of
+    split rows and inside its run of other rows, with block counts
+    descending in every run."""
+    s = CASES[name]()
+    g = GbIlu(device=-1)
+    g.analyze(s.rowptr, s.colind)
+    nc, color, perm, cp = g.ordering()
+    order = g.device_order()
+    iperm = np.empty(s.nb, np.int64)
+    iperm[perm] = np.arange(s.nb)
+    width = np.diff(s.rowptr)
+    # split run of each color: the rows the permuted order puts first
+    A = sp.csr_matrix((np.ones(len(s.colind)), s.colind, s.rowptr), shape=(s.nb, s.nb)).tocoo()
+    higher = np.zeros(s.nb, bool)
+    higher[A.row[color[A.col] > color[A.row]]] = True
+    higher[A.col[color[A.row] > color[A.col]]] = True
+    for c in range(nc):
+        a, b = cp[c], cp[c + 1]
+        k = a + int(higher[perm[a:b]].sum())
+        for lo, hi in ((a, k), (k, b)):
+            assert sorted(order[lo:hi]) == sorted(perm[lo:hi])
+            w = width[order[lo:hi]]
+            assert np.all(np.diff(w) <= 0)
+            # ties keep the permuted order
+            pos = iperm[order[lo:hi]]
+            same = np.diff(w) == 0
+            assert np.all(np.diff(pos)[same] > 0)
