@@ -409,15 +409,22 @@ struct Phase {
   __host__ __device__ bool uses_d() const { return has_d || (to_y && final_d); }
 };
 
+// d0 a0 + d1 a1 + d2 a2 in one fixed operation order (every path that
+// applies a D block uses it, so they agree bit for bit)
+template <typename T>
+__device__ __forceinline__ T dot3(T d0, T d1, T d2, T a0, T a1, T a2) {
+  return fma(d2, a2, fma(d1, a1, d0 * a0));
+}
+
 // (a0, a1, a2) <- D (a0, a1, a2) with D at d[e*32], e = 0..8 (row-major)
 template <typename V, typename T, bool GLOBAL>
 __device__ __forceinline__ void apply_dp(const V *d, T &a0, T &a1, T &a2) {
   T dd[9];
 #pragma unroll
   for (int e = 0; e < 9; ++e) dd[e] = GLOBAL ? (T)ldg_stream(d + e * 32) : (T)d[e * 32];
-  const T z0 = dd[0] * a0 + dd[1] * a1 + dd[2] * a2;
-  const T z1 = dd[3] * a0 + dd[4] * a1 + dd[5] * a2;
-  const T z2 = dd[6] * a0 + dd[7] * a1 + dd[8] * a2;
+  const T z0 = dot3(dd[0], dd[1], dd[2], a0, a1, a2);
+  const T z1 = dot3(dd[3], dd[4], dd[5], a0, a1, a2);
+  const T z2 = dot3(dd[6], dd[7], dd[8], a0, a1, a2);
   a0 = z0; a1 = z1; a2 = z2;
 }
 
@@ -563,11 +570,22 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
 // size, so rounds never straddle launches. One atomic and one poll per CTA
 // instead of fence + atomic + fence + atomic. Returns false after a timed-out
 // wait.
-__device__ __forceinline__ bool grid_barrier(Ctl *c) {
+// late: this thread's own wait before the barrier ran out; if any thread of
+// the CTA says so, the CTA still takes part in the barrier (the others do
+// not wait for it in vain), marks the run failed and gets false.
+__device__ __forceinline__ void mark_stage_timeout(Ctl *c) {
+  atomicExch(&c->bar_fail, 2);
+  c->status = ST_TIMEOUT;
+  __threadfence();
+  atomicExch(&c->done, 1);
+}
+
+__device__ __forceinline__ bool grid_barrier(Ctl *c, bool late = false) {
   __shared__ int ok;
-  __syncthreads();
+  const int any_late = __syncthreads_or(late);
   if (threadIdx.x == 0) {
-    ok = 1;
+    ok = !any_late;
+    if (any_late) mark_stage_timeout(c);
     __threadfence();   // the CTA's writes (ordered by bar.sync) before the ticket
     const unsigned int ticket = atom_add_release(&c->bar_count, 1u);
     const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x;
@@ -627,6 +645,48 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
   phase_store<V, T, false>(P, row, sd + lane, a0, a1, a2, ybuf, hat);
 }
 
+// Component c of one staged row: own_c - sum_k B_k[c,:] y_k with the FMA
+// sequence of that component in staged_row, so a row whose three components
+// are computed by three warps gets the same bits.
+template <typename V, typename T>
+__device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lane, int w,
+                                         const V *sv, const int *sc, const T *src, const T *ybuf,
+                                         const T *hat) {
+  constexpr int SB = sizeof(T) == 8 ? 4 : 8;
+  const T *own = P.own_y ? ybuf : src;
+  const T *nbr = P.nbr_hat ? hat : ybuf;
+  T a = __ldcg(own + 3 * row + c);
+  for (int k0 = 0; k0 < w; k0 += SB) {
+    int cc[SB];
+    T y[SB][3];
+#pragma unroll
+    for (int j = 0; j < SB; ++j) cc[j] = (k0 + j < w) ? sc[(k0 + j) * 32 + lane] : -1;
+#pragma unroll
+    for (int j = 0; j < SB; ++j)
+      if (cc[j] >= 0) {
+        const T *xs = cc[j] < P.src_rows ? src : nbr;
+        y[j][0] = __ldcg(xs + 3 * cc[j]);
+        y[j][1] = __ldcg(xs + 3 * cc[j] + 1);
+        y[j][2] = __ldcg(xs + 3 * cc[j] + 2);
+      }
+#pragma unroll
+    for (int j = 0; j < SB; ++j)
+      if (cc[j] >= 0) {
+        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + 3 * c * 32 + lane;
+        a = fma(-(T)b[0], y[j][0], a);
+        a = fma(-(T)b[32], y[j][1], a);
+        a = fma(-(T)b[64], y[j][2], a);
+      }
+  }
+  return a;
+}
+
+// Warps per CTA of the single-launch apply that work in groups of three on
+// the FP64 staged steps (one warp per row component)
+template <typename T> __host__ __device__ constexpr int comp_groups() {
+  return coop_threads<T>() / 32 / 3;
+}
+
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
 // launch, a grid barrier between consecutive steps. Vector loads go through
 // L2 because earlier steps of the same launch wrote them on other SMs.
@@ -641,6 +701,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
   __shared__ uint64_t stage_bar;
   __shared__ StageEntry stage_tab[kMaxStage];
   __shared__ int stage_n;
+  __shared__ T xch[sizeof(T) == 8 ? comp_groups<T>() : 1][3][32];   // FP64 component exchange
   if (ctl->done) return;
   bool staged_ready = false;
   if (sp.enabled) {
@@ -670,41 +731,108 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
   }
   constexpr int NT = coop_threads<T>();
   const int stride = gridDim.x * NT;
-  for (int q = 0; q < ph.n; ++q) {
+  // Every thread acquires the completed bulk copies itself, with a bounded
+  // wait, just before the grid barrier that precedes the first staged step
+  // (the copies finished long before); the barrier's own CTA-wide sync
+  // then makes a wait that ran out a failure of the whole CTA.
+  int first_staged = ph.n;
+  if (sp.enabled)
+    for (int q = 0; q < ph.n; ++q)
+      if (ph.p[q].staged) { first_staged = q; break; }
+  auto copies_late = [&]() {
+    unsigned int spins = 0;
+    while (!mbar_try_wait(&stage_bar, 0))
+      if (++spins > kStageSpins) return true;
+    return false;
+  };
+  bool run = true;
+  if (first_staged == 0) {
+    if (__syncthreads_or(copies_late())) {
+      if (threadIdx.x == 0) mark_stage_timeout(ctl);
+      run = false;
+    } else {
+      staged_ready = true;
+    }
+  }
+  for (int q = 0; run && q < ph.n; ++q) {
     if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
     const Phase P = ph.p[q];
     const int *off = P.mat ? off2 : off1;
     const int *col = P.mat ? col2 : col1;
     const V *val = P.mat ? val2 : val1;
     if (P.staged && sp.enabled) {
-      if (!staged_ready) {
-        // bounded wait for this CTA's bulk copies
-        unsigned int spins = 0;
-        while (!mbar_try_wait(&stage_bar, 0)) {
-          if (++spins > kStageSpins) {
-            atomicExch(&ctl->bar_fail, 2);
-            ctl->status = ST_TIMEOUT;
-            __threadfence();
-            atomicExch(&ctl->done, 1);
-            // the copies target this CTA's shared memory: give them a second
-            // bounded wait before leaving
-            for (unsigned int k = 0; k < kStageSpins && !mbar_try_wait(&stage_bar, 0); ++k) {}
-            return;
-          }
-        }
-        staged_ready = true;
-      }
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int e = warp; e < stage_n; e += NT / 32) {
-        const StageEntry E = stage_tab[e];
-        if (E.q != q) continue;
-        const int r = 32 * E.j + lane;
-        if (r >= P.nrows) continue;
-        const V *sv = reinterpret_cast<const V *>(stage_smem + E.pos);
-        const int *sc = reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
-        const V *sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
-                                                  E.w * 32 * sizeof(int));
-        staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
+      if constexpr (sizeof(T) == 8) {
+        // FP64: three warps per slice, one per row component. A small step
+        // gives each SM one or two slices, and one warp's FP64 instructions
+        // issue at one per 64 cycles whatever the number of active lanes,
+        // so a slice's 9 FMA per block on one warp is the step's critical
+        // path; split by component it is a third of that. The entries of a
+        // step are contiguous in the CTA's table (the host adds them step
+        // by step).
+        constexpr int G = comp_groups<T>();
+        const int grp = warp / 3, c = warp - 3 * grp;
+        int e0 = 0;
+        while (e0 < stage_n && stage_tab[e0].q < q) ++e0;
+        int e1 = e0;
+        while (e1 < stage_n && stage_tab[e1].q == q) ++e1;
+        for (int base = e0; base < e1; base += G) {
+          const int e = base + grp;
+          const bool act = grp < G && e < e1;
+          bool valid = false;
+          int row = 0;
+          T a = 0;
+          const V *sd = nullptr;
+          if (act) {
+            const StageEntry E = stage_tab[e];
+            const int r = 32 * E.j + lane;
+            valid = r < P.nrows;
+            row = P.row0 + r;
+            const V *sv = reinterpret_cast<const V *>(stage_smem + E.pos);
+            const int *sc =
+                reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
+            sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
+                                             E.w * 32 * sizeof(int)) + lane;
+            if (valid) a = staged_comp<V, T>(P, c, row, lane, E.w, sv, sc, src, ybuf, hat);
+          }
+          // the D products need all three components: exchange them through
+          // shared memory (the step decides for the whole CTA)
+          if (P.has_d) {
+            if (grp < G) xch[grp][c][lane] = a;
+            __syncthreads();
+            if (act && valid)
+              a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
+                          xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
+            __syncthreads();
+          }
+          bool fin = true;
+          if (P.to_y) {
+            if (valid) ybuf[3 * row + c] = a;
+            fin = row >= P.final0;
+            if (P.final_d) {
+              if (grp < G) xch[grp][c][lane] = a;
+              __syncthreads();
+              if (act && valid && fin)
+                a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
+                            xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
+              __syncthreads();
+            }
+          }
+          if (valid && fin) hat[3 * row + c] = a;
+        }
+      } else {
+        for (int e = warp; e < stage_n; e += NT / 32) {
+          const StageEntry E = stage_tab[e];
+          if (E.q != q) continue;
+          const int r = 32 * E.j + lane;
+          if (r >= P.nrows) continue;
+          const V *sv = reinterpret_cast<const V *>(stage_smem + E.pos);
+          const int *sc =
+              reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
+          const V *sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
+                                                    E.w * 32 * sizeof(int));
+          staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
+        }
       }
     } else {
       // slice j of the step goes to CTA j % grid: the device numbering puts
@@ -719,7 +847,11 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       }
     }
     bool ok = true;
-    if (q + 1 < ph.n) ok = grid_barrier(ctl);
+    if (q + 1 < ph.n) {
+      const bool before_staged = q + 1 == first_staged;
+      ok = grid_barrier(ctl, before_staged && copies_late());
+      if (ok && before_staged) staged_ready = true;
+    }
     if (ok && ph.trace && q + 1 == ph.n) {
       // the end of the last phase: after every CTA finished it
       ok = grid_barrier(ctl);
@@ -728,8 +860,8 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
     if (!ok) break;
   }
   if (sp.enabled && !staged_ready) {
-    // no staged step ran in this CTA (e.g. the last steps were not staged):
-    // still wait, bounded, for its bulk copies before the CTA exits
+    // the copies were never acquired (a failed run): still wait, bounded,
+    // for them before the CTA exits
     for (unsigned int k = 0; k < kStageSpins && !mbar_try_wait(&stage_bar, 0); ++k) {}
   }
 }
