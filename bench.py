@@ -232,11 +232,16 @@ def gpu_bench(args, world, rank, local):
     # the dominant kernel of the FP64 solve by device-time share (ncu launch
     # list, profiles/): the single-launch ILU0 apply
     dom = kern["ilu64"]
+    # its FP64 floor: 9 FMA per block of L, U and D^-1 at the FP64 rate
+    # measured on GB300 (1.68 FMA lanes per clock per SM, 2.07 GHz)
+    fp64_fma_per_s = 1.68 * torch.cuda.get_device_properties(local).multi_processor_count * 2.07e9
+    fp64_floor_us = 9 * (st["nnzb_lower"] + st["nnzb_upper"] + st["nb"]) / fp64_fma_per_s * 1e6
     roofline = {"bound": "hbm", "kernel": "k_ilu_coop<double> (ILU0 L+U sweeps, FP64)",
                 "achieved": dom["gbs"], "peak": peak, "unit": "GB/s",
                 "frac": dom["gbs"] / peak, "traffic": traffic,
                 "peak_kind": peak_kind, "alg_bytes_per_launch": dom["alg_bytes"],
-                "fp64_pipe_floor_us": 9 * (st["nnzb_lower"] + st["nnzb_upper"] + st["nb"]) / 0.59e12 * 1e6}
+                "fp64_pipe_floor_us": fp64_floor_us,
+                "fp64_floor_frac": fp64_floor_us / (dom["ms"] * 1e3)}
 
     extra = {}
     if not args.quick and rank == 0:
