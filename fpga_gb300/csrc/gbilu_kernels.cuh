@@ -304,14 +304,18 @@ enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3, 
 // omega = (y,w)/(y,y) (step 10). TRUE: y = b - A x and ||y|| into
 // Ctl::true_norm, only when a residual replacement is due.
 // V: matrix value type, T: vector type.
-// CTAs per SM the register budget must allow: the FP32 SpMV is HBM-bound
-// and gains from a third CTA (80 registers, no spills); the FP64 one is
-// bound by the FP64 pipe and keeps two
+// CTAs per SM the register budget must allow: three in both precisions
+// (80 registers, no spills). The FP32 SpMV is HBM-bound and gains from the
+// third CTA; in FP64 the plain mode fits three anyway, and the modes with
+// fused dots (88-90 registers with two) gain 2.5 % per solve iteration.
 #ifndef GBILU_SPMV32_MINB
 #define GBILU_SPMV32_MINB 3
 #endif
+#ifndef GBILU_SPMV64_MINB
+#define GBILU_SPMV64_MINB 3
+#endif
 template <typename V, typename T, int MODE>
-__global__ void __launch_bounds__(kThreads, sizeof(V) == 4 ? GBILU_SPMV32_MINB : 2)
+__global__ void __launch_bounds__(kThreads, sizeof(V) == 4 ? GBILU_SPMV32_MINB : GBILU_SPMV64_MINB)
 k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
        T *__restrict__ y, const T *__restrict__ w, double *partials) {
