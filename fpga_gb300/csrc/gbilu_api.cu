@@ -223,6 +223,10 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
       p.nbr_hat = 1;
     }
   }
+  // consecutive single-slice steps (the few rows of the top colors) run on
+  // CTA 0, which orders them with a CTA barrier: one grid barrier less each
+  for (int q = 0; q + 1 < pl.n; ++q)
+    pl.p[q].local_after = pl.p[q].nrows <= kSliceRows && pl.p[q + 1].nrows <= kSliceRows;
   return pl;
 }
 
@@ -258,8 +262,10 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
     if (P.nrows > kSmallRows) continue;
     const SlicedMatrix &m = t == 0 ? (P.mat ? an.U : an.L) : (P.mat ? an.Lt : an.Ut);
     const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
+    // steps linked by a CTA barrier (local_after) all run on CTA 0
+    const bool local = P.local_after || (q > 0 && pl.p[q - 1].local_after);
     for (int j = 0; j < nsl; ++j) {
-      const int b = (j + q) % grid;
+      const int b = local ? 0 : (j + q) % grid;
       const int w = m.off[P.slice0 + j + 1] - m.off[P.slice0 + j];
       const long long sz = (long long)w * 9 * 32 * sizeof(V) + (long long)w * 32 * sizeof(int) +
                            (P.uses_d() ? 9 * 32 * (long long)sizeof(V) : 0);
@@ -1250,9 +1256,10 @@ int gbilu_schedule(void *handle, int transpose, int cap, int *nsteps, int *steps
   if (nsteps) *nsteps = pl.n;
   for (int q = 0; q < pl.n && q < cap && steps; ++q) {
     const Phase &P = pl.p[q];
-    // every step starts at a slice edge and ends with a grid barrier
+    // every step starts at a slice edge and ends with a grid barrier, or a
+    // CTA barrier when it and the next step run on CTA 0 alone
     const int v[13] = {P.row0, P.nrows, P.slice0, 0, P.mat, P.has_d, P.own_y, P.nbr_hat,
-                       P.src_rows, P.to_y, P.final0, P.final_d, 1};
+                       P.src_rows, P.to_y, P.final0, P.final_d, P.local_after ? 2 : 1};
     memcpy(steps + 13 * q, v, sizeof v);
   }
   return GBILU_OK;

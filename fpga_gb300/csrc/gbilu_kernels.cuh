@@ -409,6 +409,8 @@ struct Phase {
   int final0;     // ... and rows from final0 on are final: hat = [D] result
   int final_d;    //     with D = D^-1 (forward) or the identity (adjoint)
   int staged;     // the step's matrix rows come from shared memory
+  int local_after;  // this step and the next have one slice each and run on
+                    // CTA 0: a CTA barrier between them instead of a grid one
   // whether a D block of the step's rows is read
   __host__ __device__ bool uses_d() const { return has_d || (to_y && final_d); }
 };
@@ -851,7 +853,9 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       }
     }
     bool ok = true;
-    if (q + 1 < ph.n) {
+    if (q + 1 < ph.n && P.local_after) {
+      __syncthreads();   // the next step reads this one's rows, all written by this CTA
+    } else if (q + 1 < ph.n) {
       const bool before_staged = q + 1 == first_staged;
       ok = grid_barrier(ctl, before_staged && copies_late());
       if (ok && before_staged) staged_ready = true;

@@ -226,7 +226,9 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
  * the analyzed pattern, a diagnostic of its schedule: per step 13 ints
  * {row0, nrows, slice0, lane0 (lane of row0 in its slice), matrix (0: first
  * sweep, 1: second), has_d, own_y, nbr_hat, src_rows, to_y, final0,
- * final_d, barrier_after (a grid barrier ends the step)}. Up to cap steps
+ * final_d, barrier_after (1: a grid barrier ends the step; 2: a CTA barrier
+ * only -- the step and the next have one slice each and run on the same
+ * CTA)}. Up to cap steps
  * are written; *nsteps gets the count. Works on host-only handles.
  * Counterpart of the reference's per-color processing order
  * (sparstition.vhd:751-756, ilu0.vhd:293-323,406-417). */

@@ -1,7 +1,9 @@
 """The step schedule of the single-launch ILU apply (gbilu_schedule), checked
 on the CPU against the sparsity pattern: every value a step reads was written
 in an earlier barrier interval (steps that share an interval are
-independent), every z row is written exactly once, every y row at most once.
+independent; a CTA barrier between two single-slice steps on one CTA counts
+as a boundary), every z row is written exactly once, every y row at most
+once.
 Runs on host-only handles (no GPU)."""
 import numpy as np
 import pytest
@@ -43,6 +45,12 @@ def test_schedule_dependencies(built_lib, name, transpose):
     wh = np.full(nb, -1)
     steps = g.schedule(transpose)
     assert steps and steps[-1]["barrier_after"] in (0, 1)
+    # a CTA barrier (2) only links two single-slice steps (both run on CTA 0),
+    # so it orders them like a grid barrier would
+    for st, nxt in zip(steps, steps[1:]):
+        if st["barrier_after"] == 2:
+            assert st["nrows"] <= 32 and nxt["nrows"] <= 32
+            assert st["lane0"] == 0 and nxt["lane0"] == 0
     k = 0
     pend_y, pend_h = [], []
     for st in steps:
