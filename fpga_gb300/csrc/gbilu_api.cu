@@ -224,9 +224,13 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
     }
   }
   // consecutive single-slice steps (the few rows of the top colors) run on
-  // CTA 0, which orders them with a CTA barrier: one grid barrier less each
-  for (int q = 0; q + 1 < pl.n; ++q)
+  // CTA 0, which orders them with a CTA barrier: one grid barrier less each;
+  // consecutive small steps, once staged, need no barrier at all: they are
+  // ordered by their data (sentinel polling in k_ilu_coop)
+  for (int q = 0; q + 1 < pl.n; ++q) {
     pl.p[q].local_after = pl.p[q].nrows <= kSliceRows && pl.p[q + 1].nrows <= kSliceRows;
+    pl.p[q].flow_after = pl.p[q].nrows <= kSmallRows && pl.p[q + 1].nrows <= kSmallRows;
+  }
   return pl;
 }
 
@@ -1256,10 +1260,12 @@ int gbilu_schedule(void *handle, int transpose, int cap, int *nsteps, int *steps
   if (nsteps) *nsteps = pl.n;
   for (int q = 0; q < pl.n && q < cap && steps; ++q) {
     const Phase &P = pl.p[q];
-    // every step starts at a slice edge and ends with a grid barrier, or a
-    // CTA barrier when it and the next step run on CTA 0 alone
+    // every step starts at a slice edge and ends with a grid barrier, a CTA
+    // barrier when it and the next step run on CTA 0 alone, or none when
+    // both are small (staged: the next step waits for the values it reads)
     const int v[13] = {P.row0, P.nrows, P.slice0, 0, P.mat, P.has_d, P.own_y, P.nbr_hat,
-                       P.src_rows, P.to_y, P.final0, P.final_d, P.local_after ? 2 : 1};
+                       P.src_rows, P.to_y, P.final0, P.final_d,
+                       P.flow_after ? 3 : P.local_after ? 2 : 1};
     memcpy(steps + 13 * q, v, sizeof v);
   }
   return GBILU_OK;

@@ -411,6 +411,8 @@ struct Phase {
   int staged;     // the step's matrix rows come from shared memory
   int local_after;  // this step and the next have one slice each and run on
                     // CTA 0: a CTA barrier between them instead of a grid one
+  int flow_after;   // this step and the next are small: when both are staged,
+                    // no barrier -- the next step waits for the values it reads
   // whether a D block of the step's rows is read
   __host__ __device__ bool uses_d() const { return has_d || (to_y && final_d); }
 };
@@ -612,30 +614,94 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c, bool late = false) {
   return ok != 0;
 }
 
+// Runs of consecutive staged steps are ordered by the data instead of grid
+// barriers: when the launch starts, every CTA sets the outputs (y and z
+// rows) of its staged rows to a sentinel, a NaN payload that arithmetic
+// never produces (its NaNs are canonical, and every staged output is an
+// arithmetic result), and a consumer that loads a sentinel loads again
+// until the producer's value is there. One memory round trip per dependency
+// instead of a barrier's fence, atomic and poll. Values are single-copy
+// atomic 4- or 8-byte words, written and polled with relaxed gpu-scope
+// accesses. Every wait is bounded: a wait that runs out marks the run failed
+// (Ctl::bar_fail = 3, status TIMEOUT) and later waits give up at once.
+__device__ __forceinline__ bool is_sentinel(double v) {
+  return __double_as_longlong(v) == (long long)0x7ff4a5a5a5a5a5a5ull;
+}
+__device__ __forceinline__ bool is_sentinel(float v) { return __float_as_uint(v) == 0x7fa5a5a5u; }
+template <typename T> __device__ __forceinline__ T sentinel_value() {
+  if constexpr (sizeof(T) == 8) return __longlong_as_double((long long)0x7ff4a5a5a5a5a5a5ull);
+  else return __uint_as_float(0x7fa5a5a5u);
+}
+__device__ __forceinline__ double ld_relaxed(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ float ld_relaxed(const float *p) {
+  float v;
+  asm volatile("ld.relaxed.gpu.global.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(double *p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(float *p, float v) {
+  asm volatile("st.relaxed.gpu.global.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+// Bounded wait for one retry round of a batch of polled loads: returns false
+// (and marks the run failed) when the wait ran out or another wait already
+// failed.
+__device__ __forceinline__ bool poll_again(Ctl *ctl, unsigned int &spins) {
+  if (++spins > kBarrierSpins || ((spins & 255) == 0 && *(volatile int *)&ctl->bar_fail)) {
+    if (!*(volatile int *)&ctl->bar_fail) {
+      atomicExch(&ctl->bar_fail, 3);
+      ctl->status = ST_TIMEOUT;
+      __threadfence();
+      atomicExch(&ctl->done, 1);
+    }
+    return false;
+  }
+  if (spins > 4) __nanosleep(32);
+  return true;
+}
+
 // One staged row (thread per row, data in shared memory): the column
 // indices come first so that all neighbour gathers of the row are in flight
 // together. Same arithmetic as phase_row.
 template <typename V, typename T>
 __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, int w, const V *sv,
                                            const int *sc, const V *sd, const T *src, T *ybuf,
-                                           T *hat) {
+                                           T *hat, Ctl *ctl) {
   constexpr int SB = sizeof(T) == 8 ? 4 : 8;   // gathers in flight per batch
   const T *own = P.own_y ? ybuf : src;
   const T *nbr = P.nbr_hat ? hat : ybuf;
-  T a0 = __ldcg(own + 3 * row), a1 = __ldcg(own + 3 * row + 1), a2 = __ldcg(own + 3 * row + 2);
+  T a0, a1, a2;
+  unsigned int spins = 0;
+  do {   // all three again while any is still a sentinel
+    a0 = ld_relaxed(own + 3 * row); a1 = ld_relaxed(own + 3 * row + 1);
+    a2 = ld_relaxed(own + 3 * row + 2);
+  } while ((is_sentinel(a0) || is_sentinel(a1) || is_sentinel(a2)) && poll_again(ctl, spins));
   for (int k0 = 0; k0 < w; k0 += SB) {
     int c[SB];
     T y[SB][3];
 #pragma unroll
     for (int j = 0; j < SB; ++j) c[j] = (k0 + j < w) ? sc[(k0 + j) * 32 + lane] : -1;
+    bool wait;
+    do {   // the whole batch again while any value is still a sentinel
+      wait = false;
 #pragma unroll
-    for (int j = 0; j < SB; ++j)
-      if (c[j] >= 0) {
-        const T *xs = c[j] < P.src_rows ? src : nbr;
-        y[j][0] = __ldcg(xs + 3 * c[j]);
-        y[j][1] = __ldcg(xs + 3 * c[j] + 1);
-        y[j][2] = __ldcg(xs + 3 * c[j] + 2);
-      }
+      for (int j = 0; j < SB; ++j)
+        if (c[j] >= 0) {
+          const T *xs = (c[j] < P.src_rows ? src : nbr) + 3 * c[j];
+          y[j][0] = ld_relaxed(xs);
+          y[j][1] = ld_relaxed(xs + 1);
+          y[j][2] = ld_relaxed(xs + 2);
+        }
+#pragma unroll
+      for (int j = 0; j < SB; ++j)
+        if (c[j] >= 0)
+          wait |= is_sentinel(y[j][0]) || is_sentinel(y[j][1]) || is_sentinel(y[j][2]);
+    } while (wait && poll_again(ctl, spins));
 #pragma unroll
     for (int j = 0; j < SB; ++j)
       if (c[j] >= 0) {
@@ -648,7 +714,14 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
         a2 = fma(-(T)b[8 * 32], y[j][2], a2);
       }
   }
-  phase_store<V, T, false>(P, row, sd + lane, a0, a1, a2, ybuf, hat);
+  if (P.has_d) apply_dp<V, T, false>(sd + lane, a0, a1, a2);
+  if (P.to_y) {
+    st_relaxed(ybuf + 3 * row, a0); st_relaxed(ybuf + 3 * row + 1, a1);
+    st_relaxed(ybuf + 3 * row + 2, a2);
+    if (row < P.final0) return;
+    if (P.final_d) apply_dp<V, T, false>(sd + lane, a0, a1, a2);
+  }
+  st_relaxed(hat + 3 * row, a0); st_relaxed(hat + 3 * row + 1, a1); st_relaxed(hat + 3 * row + 2, a2);
 }
 
 // Component c of one staged row: own_c - sum_k B_k[c,:] y_k with the FMA
@@ -657,24 +730,36 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
 template <typename V, typename T>
 __device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lane, int w,
                                          const V *sv, const int *sc, const T *src, const T *ybuf,
-                                         const T *hat) {
+                                         const T *hat, Ctl *ctl) {
   constexpr int SB = sizeof(T) == 8 ? 4 : 8;
   const T *own = P.own_y ? ybuf : src;
   const T *nbr = P.nbr_hat ? hat : ybuf;
-  T a = __ldcg(own + 3 * row + c);
+  T a;
+  unsigned int spins = 0;
+  do {
+    a = ld_relaxed(own + 3 * row + c);
+  } while (is_sentinel(a) && poll_again(ctl, spins));
   for (int k0 = 0; k0 < w; k0 += SB) {
     int cc[SB];
     T y[SB][3];
 #pragma unroll
     for (int j = 0; j < SB; ++j) cc[j] = (k0 + j < w) ? sc[(k0 + j) * 32 + lane] : -1;
+    bool wait;
+    do {   // the whole batch again while any value is still a sentinel
+      wait = false;
 #pragma unroll
-    for (int j = 0; j < SB; ++j)
-      if (cc[j] >= 0) {
-        const T *xs = cc[j] < P.src_rows ? src : nbr;
-        y[j][0] = __ldcg(xs + 3 * cc[j]);
-        y[j][1] = __ldcg(xs + 3 * cc[j] + 1);
-        y[j][2] = __ldcg(xs + 3 * cc[j] + 2);
-      }
+      for (int j = 0; j < SB; ++j)
+        if (cc[j] >= 0) {
+          const T *xs = (cc[j] < P.src_rows ? src : nbr) + 3 * cc[j];
+          y[j][0] = ld_relaxed(xs);
+          y[j][1] = ld_relaxed(xs + 1);
+          y[j][2] = ld_relaxed(xs + 2);
+        }
+#pragma unroll
+      for (int j = 0; j < SB; ++j)
+        if (cc[j] >= 0)
+          wait |= is_sentinel(y[j][0]) || is_sentinel(y[j][1]) || is_sentinel(y[j][2]);
+    } while (wait && poll_again(ctl, spins));
 #pragma unroll
     for (int j = 0; j < SB; ++j)
       if (cc[j] >= 0) {
@@ -691,6 +776,12 @@ __device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lan
 // the FP64 staged steps (one warp per row component)
 template <typename T> __host__ __device__ constexpr int comp_groups() {
   return coop_threads<T>() / 32 / 3;
+}
+
+// The three warps of component group g (named barrier 1 + g; 0 is
+// __syncthreads)
+__device__ __forceinline__ void group_sync(int g) {
+  asm volatile("bar.sync %0, 96;" ::"r"(1 + g) : "memory");
 }
 
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
@@ -734,6 +825,20 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       if (P.uses_d())
         bulk_g2s(dst + vb + cb, dmat + (size_t)s * 9 * 32, (uint32_t)(9 * 32 * sizeof(V)), &stage_bar);
     }
+    // sentinels into the outputs of this CTA's staged rows; a grid barrier
+    // separates them from every consumer
+    const T sent = sentinel_value<T>();
+    for (int e = threadIdx.x >> 5; e < stage_n; e += coop_threads<T>() / 32) {
+      const StageEntry E = stage_tab[e];
+      const Phase &P = ph.p[E.q];
+      const int r = 32 * E.j + (threadIdx.x & 31);
+      if (r >= P.nrows) continue;
+      const int row = P.row0 + r;
+      if (P.to_y)
+        for (int k = 0; k < 3; ++k) st_relaxed(ybuf + 3 * row + k, sent);
+      if (!P.to_y || row >= P.final0)
+        for (int k = 0; k < 3; ++k) st_relaxed(hat + 3 * row + k, sent);
+    }
   }
   constexpr int NT = coop_threads<T>();
   const int stride = gridDim.x * NT;
@@ -753,12 +858,9 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
   };
   bool run = true;
   if (first_staged == 0) {
-    if (__syncthreads_or(copies_late())) {
-      if (threadIdx.x == 0) mark_stage_timeout(ctl);
-      run = false;
-    } else {
-      staged_ready = true;
-    }
+    // every step is small: the sentinels need a grid barrier before any step
+    run = grid_barrier(ctl, copies_late());
+    staged_ready = run;
   }
   for (int q = 0; run && q < ph.n; ++q) {
     if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
@@ -799,32 +901,34 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
                 reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
             sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
                                              E.w * 32 * sizeof(int)) + lane;
-            if (valid) a = staged_comp<V, T>(P, c, row, lane, E.w, sv, sc, src, ybuf, hat);
+            if (valid) a = staged_comp<V, T>(P, c, row, lane, E.w, sv, sc, src, ybuf, hat, ctl);
           }
-          // the D products need all three components: exchange them through
-          // shared memory (the step decides for the whole CTA)
+          if (!act) continue;   // the whole group (same e) skips the round
+          // the D products need all three components: the group's warps
+          // exchange them through shared memory, synchronised by the group's
+          // own named barrier (warps of other groups may be in other steps)
           if (P.has_d) {
-            if (grp < G) xch[grp][c][lane] = a;
-            __syncthreads();
-            if (act && valid)
+            xch[grp][c][lane] = a;
+            group_sync(grp);
+            if (valid)
               a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
                           xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
-            __syncthreads();
+            group_sync(grp);
           }
           bool fin = true;
           if (P.to_y) {
-            if (valid) ybuf[3 * row + c] = a;
+            if (valid) st_relaxed(ybuf + 3 * row + c, a);
             fin = row >= P.final0;
             if (P.final_d) {
-              if (grp < G) xch[grp][c][lane] = a;
-              __syncthreads();
-              if (act && valid && fin)
+              xch[grp][c][lane] = a;
+              group_sync(grp);
+              if (valid && fin)
                 a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
                             xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
-              __syncthreads();
+              group_sync(grp);
             }
           }
-          if (valid && fin) hat[3 * row + c] = a;
+          if (valid && fin) st_relaxed(hat + 3 * row + c, a);
         }
       } else {
         for (int e = warp; e < stage_n; e += NT / 32) {
@@ -837,7 +941,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
               reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
           const V *sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
                                                     E.w * 32 * sizeof(int));
-          staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat);
+          staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat, ctl);
         }
       }
     } else {
@@ -853,7 +957,9 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       }
     }
     bool ok = true;
-    if (q + 1 < ph.n && P.local_after) {
+    if (q + 1 < ph.n && P.flow_after && P.staged && ph.p[q + 1].staged && sp.enabled) {
+      // data-ordered: the next step waits for the values it reads
+    } else if (q + 1 < ph.n && P.local_after) {
       __syncthreads();   // the next step reads this one's rows, all written by this CTA
     } else if (q + 1 < ph.n) {
       const bool before_staged = q + 1 == first_staged;

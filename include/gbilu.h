@@ -228,7 +228,8 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
  * sweep, 1: second), has_d, own_y, nbr_hat, src_rows, to_y, final0,
  * final_d, barrier_after (1: a grid barrier ends the step; 2: a CTA barrier
  * only -- the step and the next have one slice each and run on the same
- * CTA)}. Up to cap steps
+ * CTA; 3: no barrier -- both steps are small, staged in shared memory, and
+ * the next one waits for each value it reads)}. Up to cap steps
  * are written; *nsteps gets the count. Works on host-only handles.
  * Counterpart of the reference's per-color processing order
  * (sparstition.vhd:751-756, ilu0.vhd:293-323,406-417). */

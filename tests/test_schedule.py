@@ -1,8 +1,9 @@
 """The step schedule of the single-launch ILU apply (gbilu_schedule), checked
 on the CPU against the sparsity pattern: every value a step reads was written
 in an earlier barrier interval (steps that share an interval are
-independent; a CTA barrier between two single-slice steps on one CTA counts
-as a boundary), every z row is written exactly once, every y row at most
+independent; a CTA barrier between two single-slice steps on one CTA, and
+the data ordering of consecutive small steps, count as boundaries), every z
+row is written exactly once, every y row at most
 once.
 Runs on host-only handles (no GPU)."""
 import numpy as np
@@ -47,10 +48,14 @@ def test_schedule_dependencies(built_lib, name, transpose):
     assert steps and steps[-1]["barrier_after"] in (0, 1)
     # a CTA barrier (2) only links two single-slice steps (both run on CTA 0),
     # so it orders them like a grid barrier would
+    # and no barrier (3) links two small steps, whose consumers wait for each
+    # value they read: every kind orders the steps
     for st, nxt in zip(steps, steps[1:]):
         if st["barrier_after"] == 2:
             assert st["nrows"] <= 32 and nxt["nrows"] <= 32
             assert st["lane0"] == 0 and nxt["lane0"] == 0
+        if st["barrier_after"] == 3:
+            assert st["nrows"] <= 16384 and nxt["nrows"] <= 16384
     k = 0
     pend_y, pend_h = [], []
     for st in steps:
