@@ -219,7 +219,9 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms,
 /* Traced ILU apply: runs the single-launch preconditioner apply (FP64, or
  * FP32 with GBILU_MIXED; forward or transposed) with device timestamps at
  * every color step and returns each step's duration in microseconds (the
- * step plus the grid barrier after it) and its row count. The GB300
+ * step plus the grid barrier after it, as CTA 0 sees it; inside a run of
+ * small steps ordered by their data, CTA 0's own progress) and its row
+ * count. The GB300
  * counterpart of the reference's periodic debug lines (solver.vhd:1106-1133),
  * per color step instead of per sampling interval. */
 /* The step list of the single-launch ILU apply (forward or transposed) for
