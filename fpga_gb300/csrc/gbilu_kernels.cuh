@@ -675,12 +675,15 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
   constexpr int SB = sizeof(T) == 8 ? 4 : 8;   // gathers in flight per batch
   const T *own = P.own_y ? ybuf : src;
   const T *nbr = P.nbr_hat ? hat : ybuf;
+  // only values of ybuf and hat can be sentinels: reads of the input src are
+  // never checked (any bit pattern there is data)
   T a0, a1, a2;
   unsigned int spins = 0;
   do {   // all three again while any is still a sentinel
     a0 = ld_relaxed(own + 3 * row); a1 = ld_relaxed(own + 3 * row + 1);
     a2 = ld_relaxed(own + 3 * row + 2);
-  } while ((is_sentinel(a0) || is_sentinel(a1) || is_sentinel(a2)) && poll_again(ctl, spins));
+  } while (P.own_y && (is_sentinel(a0) || is_sentinel(a1) || is_sentinel(a2)) &&
+           poll_again(ctl, spins));
   for (int k0 = 0; k0 < w; k0 += SB) {
     int c[SB];
     T y[SB][3];
@@ -699,7 +702,7 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
         }
 #pragma unroll
       for (int j = 0; j < SB; ++j)
-        if (c[j] >= 0)
+        if (c[j] >= P.src_rows)
           wait |= is_sentinel(y[j][0]) || is_sentinel(y[j][1]) || is_sentinel(y[j][2]);
     } while (wait && poll_again(ctl, spins));
 #pragma unroll
@@ -736,9 +739,9 @@ __device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lan
   const T *nbr = P.nbr_hat ? hat : ybuf;
   T a;
   unsigned int spins = 0;
-  do {
+  do {   // (src is never checked: see staged_row)
     a = ld_relaxed(own + 3 * row + c);
-  } while (is_sentinel(a) && poll_again(ctl, spins));
+  } while (P.own_y && is_sentinel(a) && poll_again(ctl, spins));
   for (int k0 = 0; k0 < w; k0 += SB) {
     int cc[SB];
     T y[SB][3];
@@ -757,7 +760,7 @@ __device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lan
         }
 #pragma unroll
       for (int j = 0; j < SB; ++j)
-        if (cc[j] >= 0)
+        if (cc[j] >= P.src_rows)
           wait |= is_sentinel(y[j][0]) || is_sentinel(y[j][1]) || is_sentinel(y[j][2]);
     } while (wait && poll_again(ctl, spins));
 #pragma unroll

@@ -92,3 +92,26 @@ def test_solve_and_adjoint(edge, precision):
         assert ra.status == 0
         assert np.linalg.norm(A.T @ lam - gv) <= tol * np.linalg.norm(gv) * (1 + 1e-6)
         assert np.abs(dA - P.grad_a(lam, x)).max() <= 1e-14 * max(np.abs(dA).max(), 1e-300)
+
+
+@pytest.mark.parametrize("transpose", [False, True])
+def test_apply_input_with_sentinel_bits(built_lib, transpose):
+    """The small color steps are ordered by their data: their outputs start
+    as a NaN sentinel that consumers wait on. An input vector that carries
+    that bit pattern is data like any other (input reads are never waited
+    on): the apply returns at once with the oracle's NaN pattern."""
+    import time
+    s = generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7)
+    P = Prepared(s)
+    p = np.random.default_rng(8).standard_normal(s.n)
+    bits = p.view(np.uint64)
+    bits[[5, 600, s.n - 4]] = np.uint64(0x7ff4a5a5a5a5a5a5)
+    with GbIlu(device=0) as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        t0 = time.perf_counter()
+        z = g.ilu_apply(p, transpose)
+        assert time.perf_counter() - t0 < 1.0
+    z_ref = P.ilu_apply(p, transpose)
+    nan = np.isnan(z_ref)
+    assert nan.any() and np.array_equal(np.isnan(z), nan)
+    assert rel(z[~nan], z_ref[~nan]) < KERNEL_TOL
