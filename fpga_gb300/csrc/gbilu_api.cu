@@ -1244,6 +1244,30 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   return GBILU_OK;
 }
 
+int gbilu_wait_probe(void *handle, int mode, int *bar_fail, int *status, double *ms) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h || (mode != 0 && mode != 1)) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  if (h->opt.device < 0) return h->fail(GBILU_NO_DEVICE, "host-only handle cannot run the probe");
+  CK(cudaSetDevice(h->opt.device));
+  Ctl *c = h->ctl.p + 1;   // the spare control block: the solve state stays as it is
+  k_ctl_init<<<1, 32, 0, h->st>>>(c, 0.0, 0, 0, 0ull);
+  const unsigned long long sent = 0x7ff4a5a5a5a5a5a5ull;   // the data-ordered steps' sentinel
+  CK(cudaMemcpyAsync(h->io64.p, &sent, sizeof sent, cudaMemcpyHostToDevice, h->st));
+  CK(cudaEventRecord(h->e0, h->st));
+  k_wait_probe<<<2, 32, 0, h->st>>>(c, mode, h->io64.p);
+  CK(cudaEventRecord(h->e1, h->st));
+  CK(cudaMemcpyAsync(h->h_ctl, c, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  CK(last_error(h));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, h->e0, h->e1));
+  if (bar_fail) *bar_fail = h->h_ctl->bar_fail;
+  if (status) *status = h->h_ctl->status;
+  if (ms) *ms = t;
+  return GBILU_OK;
+}
+
 int gbilu_device_order(void *handle, int *order) {
   Handle *h = static_cast<Handle *>(handle);
   if (!h || !order) return GBILU_BAD_INPUT;

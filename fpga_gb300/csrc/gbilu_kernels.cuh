@@ -983,6 +983,24 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
   }
 }
 
+// Self-test of the bounded waits (failure detection without a GPU fault):
+// mode 0, a grid barrier that one of the two CTAs never reaches; mode 1, a
+// data-ordered load of a word that stays the sentinel. Both waits run out
+// after their poll limit, mark the run failed (Ctl::bar_fail 1 or 3,
+// status TIMEOUT) and return, leaving the context usable.
+__global__ void k_wait_probe(Ctl *ctl, int mode, const double *word) {
+  if (mode == 0) {
+    if (blockIdx.x == 1) return;   // never arrives
+    grid_barrier(ctl);
+  } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned int spins = 0;
+    double v;
+    do {
+      v = ld_relaxed(word);
+    } while (is_sentinel(v) && poll_again(ctl, spins));
+  }
+}
+
 // --------------------------------------------------------------------------
 // fused vector kernels (grid-stride over the n unknowns)
 // --------------------------------------------------------------------------

@@ -94,6 +94,8 @@ def load():
     L.gbilu_analyze.argtypes = [VP, C.c_int, I32P, I32P]
     L.gbilu_get_ordering.argtypes = [VP, C.POINTER(C.c_int), VP, VP, VP]
     L.gbilu_device_order.argtypes = [VP, VP]
+    L.gbilu_wait_probe.argtypes = [VP, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_double)]
     L.gbilu_factor.argtypes = [VP, F64P]
     L.gbilu_get_factors.argtypes = [VP, VP, VP]
     L.gbilu_solve.argtypes = [VP, VP, VP, C.c_double, C.c_int, C.POINTER(Result)]
@@ -199,6 +201,14 @@ class GbIlu:
         self._check(self.L.gbilu_get_ordering(self.h, C.byref(nc), color.ctypes.data,
                                               perm.ctypes.data, cp.ctypes.data))
         return nc.value, color, perm, cp
+
+    def wait_probe(self, mode):
+        """Runs a device wait that never completes (0: grid barrier, 1: data
+        wait) and returns what its bounded timeout reported."""
+        bf, st, ms = C.c_int(), C.c_int(), C.c_double()
+        self._check(self.L.gbilu_wait_probe(self.h, int(mode), C.byref(bf), C.byref(st),
+                                            C.byref(ms)))
+        return {"bar_fail": bf.value, "status": st.value, "ms": ms.value}
 
     def device_order(self):
         """Input row held at each device row (the numbering of the device

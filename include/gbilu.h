@@ -154,6 +154,17 @@ int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind);
 int gbilu_get_ordering(void *handle, int *ncolors, int *color, int *perm,
                        int *color_ptr);
 
+/* Self-test of the device waits' bounds (failure detection without a GPU
+ * fault): mode 0 runs a grid barrier that one of its two CTAs never reaches,
+ * mode 1 a data-ordered load of a word that stays the sentinel. The wait
+ * runs out after its poll limit (about a second or two), and the probe
+ * reports what the solve kernels would report: *bar_fail (1: barrier, 3:
+ * data wait), *status (GBILU_TIMEOUT) and the device time in *ms. The
+ * handle's solve state is untouched and stays usable. Counterpart of the
+ * reference's kernel watchdog (abort_cycles, reported as kernel_aborted by
+ * bicgstab_utils.cpp:93-129). */
+int gbilu_wait_probe(void *handle, int mode, int *bar_fail, int *status, double *ms);
+
 /* The numbering of the device vectors and sliced layouts: order[d] = input
  * row held at device row d. It keeps perm's color ranges and each color's
  * leading rows with a higher-colored neighbour, and inside each of these
