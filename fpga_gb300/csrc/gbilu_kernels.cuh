@@ -805,7 +805,10 @@ __device__ __forceinline__ void group_sync(int g) {
 }
 
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
-// launch, a grid barrier between consecutive steps. Vector loads go through
+// launch. Consecutive steps are separated by a grid barrier, by a CTA
+// barrier (two single-slice steps on CTA 0), or by nothing at all inside a
+// run of staged steps, whose consumers wait for the values they read
+// (sentinel outputs, see is_sentinel). Vector loads go through
 // L2 because earlier steps of the same launch wrote them on other SMs.
 // Staged small steps read their matrix data from shared memory.
 template <typename V, typename T>

@@ -76,7 +76,8 @@ typedef struct {
   int max_outer;      /* mixed: refinement step limit */
   int verbose;        /* 0 quiet, 1 INFO lines on stdout */
   int sweep_mode;     /* 1: the whole ILU0 apply is one cooperative launch
-                         with a grid barrier between colors (default);
+                         (default): grid barriers around the large
+                         colors, the small ones ordered by their data;
                          0: one launch per color */
   int factor_on_device; /* 1: gbilu_factor permutes and ILU0-factors on the
                          GPU (color-parallel, bit-identical to the host
