@@ -126,13 +126,15 @@ __device__ __forceinline__ bool grid_sum(double (&v)[NV], double *partials,
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int j = 0; j < NV; ++j) partials[(size_t)j * gridDim.x + blockIdx.x] = v[j];
-    __threadfence();
-    const unsigned int prev = atomicAdd(counter, 1u);
+    // acquire-release arrival: releases this thread's partials and, in the
+    // last CTA, acquires everyone's (the CTA barrier below passes that on to
+    // its other threads); no separate fences
+    unsigned int prev;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(prev) : "l"(counter) : "memory");
     last = (prev == gridDim.x - 1);
   }
   __syncthreads();
   if (!last) return false;
-  __threadfence();
   double acc[NV];
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
