@@ -286,7 +286,8 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
   }
   h->stage[f][t] = StagePlan{nullptr, nullptr, 0};
   h->stage_bytes[f][t] = 0;
-  if (most_n == 0 || most > kStageBudget || most_n > (size_t)kMaxStage) {
+  if (!h->opt.stage_small_steps || most_n == 0 || most > kStageBudget ||
+      most_n > (size_t)kMaxStage) {
     for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
     return GBILU_OK;
   }
@@ -906,6 +907,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->factor_on_device = 0;
   o->mixed_scheme = 0;
   o->ru_delta = 0.1;
+  o->stage_small_steps = 1;
   return GBILU_OK;
 }
 

@@ -27,7 +27,7 @@ class Options(C.Structure):
                 ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
                 ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
                 ("factor_on_device", C.c_int), ("mixed_scheme", C.c_int),
-                ("ru_delta", C.c_double)]
+                ("ru_delta", C.c_double), ("stage_small_steps", C.c_int)]
 
 
 class Result(C.Structure):
@@ -131,7 +131,7 @@ class GbIlu:
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
                  timeout_ms=0.0, inner_tol=1e-1, inner_maxit=500, max_outer=30,
                  verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
-                 ru_delta=0.1):
+                 ru_delta=0.1, stage_small_steps=True):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -148,6 +148,7 @@ class GbIlu:
         o.factor_on_device = int(factor_on_device)
         o.mixed_scheme = mixed_scheme
         o.ru_delta = ru_delta
+        o.stage_small_steps = int(stage_small_steps)
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:

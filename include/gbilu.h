@@ -89,6 +89,11 @@ typedef struct {
                          ru_delta, x accumulated in FP64, stop on the FP64
                          residual */
   double ru_delta;    /* mixed scheme 1: replacement threshold (default 0.1) */
+  int stage_small_steps; /* 1 (default): the single-launch apply copies the
+                         small color steps' matrix slices into shared memory
+                         when it starts and orders those steps by their data;
+                         0: they read global memory and are separated by grid
+                         barriers, like the large steps (same results) */
 } gbilu_options;
 
 typedef struct {
