@@ -82,6 +82,9 @@ struct Handle {
   int sm_count = 0;
   cudaStream_t st = nullptr, cap = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // host-buffer solves move b on aux while the initial SpMV runs on st
+  cudaStream_t aux = nullptr;
+  cudaEvent_t e_b = nullptr;
   DevBuf<int2> srows;
   // perm/iperm: device row <-> input row (the vectors of a solve);
   // fperm: permuted row -> input row (the pattern-ordered gradient);
@@ -583,6 +586,8 @@ int setup_device(Handle *h) {
   if (!h->st) {
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->e_b, cudaEventDisableTiming));
     CK(cudaEventCreate(&h->e0));
     CK(cudaEventCreate(&h->e1));
     CK(cudaMallocHost(&h->h_ctl, sizeof(Ctl)));
@@ -729,18 +734,21 @@ int check_solve_ready(Handle *h) {
 // FP64 BiCGSTAB on the permuted vectors: b in h->b64, x in v64.x.
 // With sync false the final Ctl is only queued for copy into h->h_ctl: the
 // caller synchronizes once at the end (no host round trip mid-solve).
+// b_ready: an event after which b64 holds b (b is moved on another stream
+// while A x0 is computed), or null when b64 is ready in stream order.
 int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long long &launches,
-            bool sync = true) {
+            bool sync = true, cudaEvent_t b_ready = nullptr) {
   const int n = 3 * h->an.nb;
   Ops<double, double> o = make_ops<double, double>(h, transpose);
   Vecs<double> &w = h->v64;
   const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
   k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, tol, h->opt.absolute_tol, maxit, tmo);
   int l = 1;
-  spmv<double, double, SPMV_RESID>(h, h->st, o, w.x.p, w.r.p, h->b64.p, l);
+  spmv<double, double, SPMV_PLAIN>(h, h->st, o, w.x.p, w.r.p, nullptr, l);   // r = A x0
   launches += l;
-  k_init_vectors<double><<<grid_for(h, n), kThreads, 0, h->st>>>(
-      h->ctl.p, n, w.r.p, w.rt.p, w.p.p);
+  if (b_ready) CK(cudaStreamWaitEvent(h->st, b_ready, 0));
+  k_init_resid<double><<<reduce_grid(h, n), kThreads, 0, h->st>>>(
+      h->ctl.p, n, h->b64.p, w.r.p, w.rt.p, w.p.p, h->partials.p);
   launches += 1;
   int rc = run_loop<double, double>(h, transpose, maxit, launches);
   if (rc) return rc;
@@ -934,6 +942,8 @@ int gbilu_destroy(void *handle) {
     release_device(h);
     cudaStreamDestroy(h->st);
     cudaStreamDestroy(h->cap);
+    cudaStreamDestroy(h->aux);
+    cudaEventDestroy(h->e_b);
     cudaEventDestroy(h->e0);
     cudaEventDestroy(h->e1);
     cudaFreeHost(h->h_ctl);
@@ -1063,31 +1073,39 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
       db = static_cast<const double *>(ab.devicePointer);
       dx = mapped_x = static_cast<double *>(ax.devicePointer);
     } else {
-      CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-      CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-      db = h->io64.p;
+      db = h->io64.p;   // staging copies below
       dx = h->io64b.p;
     }
   }
+  // The FP64 solve needs b only after A x0 (k_init_resid): from host
+  // buffers, b moves on the auxiliary stream while the SpMV runs.
+  const bool fp64 = h->opt.precision != GBILU_MIXED;
+  const bool overlap_b = fp64 && !device_ptrs;
+  cudaStream_t sb = overlap_b ? h->aux : h->st;
+  if (overlap_b) CK(cudaStreamWaitEvent(h->aux, h->e0, 0));
+  if (!device_ptrs && !mapped_x) {
+    CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, sb));
+    CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  }
   if (mapped_x) {
     // host side read in order, device side written permuted
-    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, db, h->b64.p);
+    k_scatter<double><<<g, kThreads, 0, sb>>>(nb, h->iperm.p, db, h->b64.p);
     k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, dx, h->v64.x.p);
   } else {
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, db, h->b64.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, sb>>>(nb, h->perm.p, db, h->b64.p, 1.0);
     k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
   }
+  if (overlap_b) CK(cudaEventRecord(h->e_b, h->aux));
   launches += 2;
   Ctl c;
   gbilu_result tmp;
   memset(&tmp, 0, sizeof tmp);
   gbilu_result *r = res ? res : &tmp;
   memset(r, 0, sizeof *r);
-  const bool fp64 = h->opt.precision != GBILU_MIXED;
   if (!fp64)
     rc = solve_mixed(h, transpose, tol, maxit, r, c, launches);
   else
-    rc = solve64(h, transpose, tol, maxit, c, launches, false);
+    rc = solve64(h, transpose, tol, maxit, c, launches, false, overlap_b ? h->e_b : nullptr);
   if (rc) return rc;
   // x back to the caller's numbering. When the initial residual already met
   // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged

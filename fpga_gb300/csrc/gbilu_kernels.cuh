@@ -1027,17 +1027,25 @@ __global__ void k_wait_probe(Ctl *ctl, int mode, const double *word) {
 // fused vector kernels (grid-stride over the n unknowns)
 // --------------------------------------------------------------------------
 
-// After step 1: rt = p = r.
+// Steps 0/1 of the FP64 solve after y = A x0 (k_spmv PLAIN into r):
+// r = b - y (the RESID epilogue's arithmetic), rt = p = r, rho = ||r||^2 and
+// the stop tests of the start. Split from the SpMV so that b can still be in
+// transit while A x0 is computed.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_init_vectors(const Ctl *ctl, int n, const T *__restrict__ r, T *__restrict__ rt,
-               T *__restrict__ p) {
-  if (ctl->done) return;
+k_init_resid(Ctl *ctl, int n, const T *__restrict__ b, T *__restrict__ r, T *__restrict__ rt,
+             T *__restrict__ p, double *partials) {
+  double d = 0.0;
+  DF f = {0.f, 0.f};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const T v = r[i];
-    rt[i] = v;
-    p[i] = v;
+    const T v = b[i] - r[i];
+    r[i] = v; rt[i] = v; p[i] = v;
+    if (sizeof(T) == 8) d += (double)v * v; else df_add_prod(f, (float)v, (float)v);
   }
+  if (sizeof(T) == 4) d = df_value(f);
+  double vv[1] = {d}, tot[1];
+  if (grid_sum<1>(vv, partials, &ctl->counter[0], tot) && threadIdx.x == 0)
+    finish_init<T>(ctl, tot[0]);
 }
 
 // Inner solves of iterative refinement start from d = 0: r = rt = p = rhs,
