@@ -107,7 +107,11 @@ struct Handle {
   cudaGraphExec_t graph_ru[2] = {nullptr, nullptr};  // mixed by replacement [transpose]
   int per_iter[2] = {0, 0};                // launches per iteration [transpose]
   long long last_launches = 0;
-  PhaseList phases[2][2];                  // color steps [fp32][transpose]
+  // color steps [fp32][transpose]: the full list (one launch per step), and
+  // the same as the single-launch apply's parameter when it fits (n = 0
+  // otherwise: more than kMaxPhases / 2 colors)
+  std::vector<Phase> steps[2][2];
+  PhaseList phases[2][2];
   StagePlan stage[2][2] = {};              // shared-memory staging of small steps
   int stage_bytes[2][2] = {};
   DevBuf<StageEntry> stage_tab[2][2];
@@ -176,14 +180,14 @@ int reduce_grid(const Handle *h, long long work) {
 // U^T sweep with D^-T over all colors, the rows without a higher-colored
 // neighbour final at once (unit diagonal of L^T); the L^T sweep covers the
 // leading rows of colors C-2..0.
-PhaseList make_phases(const Analysis &an, bool transpose) {
-  PhaseList pl;
-  pl.n = 0;
-  pl.trace = 0;
+std::vector<Phase> make_steps(const Analysis &an, bool transpose) {
+  std::vector<Phase> st;
   const int C = an.ncolors;
+  st.reserve(2 * (size_t)C);
   auto rows = [&](int c) { return an.color_ptr[c + 1] - an.color_ptr[c]; };
   auto add = [&](int c, int mat, int nrows) -> Phase & {
-    Phase &p = pl.p[pl.n++];
+    st.emplace_back();
+    Phase &p = st.back();
     p = Phase{};
     p.row0 = an.color_ptr[c];
     p.nrows = nrows;
@@ -194,7 +198,7 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
   if (!transpose) {
     if (C == 1) {   // no couplings: z = D^-1 src
       add(0, 1, rows(0)).has_d = 1;
-      return pl;
+      return st;
     }
     for (int c = 1; c < C; ++c) {
       Phase &p = add(c, 0, rows(c));
@@ -230,10 +234,20 @@ PhaseList make_phases(const Analysis &an, bool transpose) {
   // CTA 0, which orders them with a CTA barrier: one grid barrier less each;
   // consecutive small steps, once staged, need no barrier at all: they are
   // ordered by their data (sentinel polling in k_ilu_coop)
-  for (int q = 0; q + 1 < pl.n; ++q) {
-    pl.p[q].local_after = pl.p[q].nrows <= kSliceRows && pl.p[q + 1].nrows <= kSliceRows;
-    pl.p[q].flow_after = pl.p[q].nrows <= kSmallRows && pl.p[q + 1].nrows <= kSmallRows;
+  for (size_t q = 0; q + 1 < st.size(); ++q) {
+    st[q].local_after = st[q].nrows <= kSliceRows && st[q + 1].nrows <= kSliceRows;
+    st[q].flow_after = st[q].nrows <= kSmallRows && st[q + 1].nrows <= kSmallRows;
   }
+  return st;
+}
+
+// The single-launch apply's parameter (n = 0 when the steps do not fit).
+PhaseList phase_list(const std::vector<Phase> &st) {
+  PhaseList pl;
+  pl.n = 0;
+  pl.trace = 0;
+  if (st.size() > (size_t)kMaxPhases) return pl;
+  for (const Phase &p : st) pl.p[pl.n++] = p;
   return pl;
 }
 
@@ -349,9 +363,7 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
     ++launches;
     return;
   }
-  const PhaseList &pl = h->phases[sizeof(T) == 4 ? 1 : 0][o.transpose ? 1 : 0];
-  for (int q = 0; q < pl.n; ++q) {
-    const Phase &P = pl.p[q];
+  for (const Phase &P : h->steps[sizeof(T) == 4 ? 1 : 0][o.transpose ? 1 : 0]) {
     k_phase<V, T><<<(unsigned)((P.nrows + kThreads - 1) / kThreads), kThreads, 0, s>>>(
         h->ctl.p, P, P.mat ? o.off2 : o.off1, P.mat ? o.col2 : o.col1, P.mat ? o.val2 : o.val1,
         o.dmat, src, o.vec->y.p, hat);
@@ -652,8 +664,10 @@ int setup_device(Handle *h) {
     h->device_bytes += (size_t)an.nnzb * 9 * 16 + (size_t)an.nb * 76;
   }
   for (int f = 0; f < 2; ++f) {
-    h->phases[f][0] = make_phases(an, false);
-    h->phases[f][1] = make_phases(an, true);
+    for (int t = 0; t < 2; ++t) {
+      h->steps[f][t] = make_steps(an, t != 0);
+      h->phases[f][t] = phase_list(h->steps[f][t]);
+    }
   }
   h->coop_grid64 = coop_grid<double, double>(h);
   h->coop_grid32 = coop_grid<float, float>(h);
@@ -1300,10 +1314,10 @@ int gbilu_schedule(void *handle, int transpose, int cap, int *nsteps, int *steps
   Handle *h = static_cast<Handle *>(handle);
   if (!h) return GBILU_BAD_INPUT;
   if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
-  const PhaseList pl = make_phases(h->an, transpose != 0);
-  if (nsteps) *nsteps = pl.n;
-  for (int q = 0; q < pl.n && q < cap && steps; ++q) {
-    const Phase &P = pl.p[q];
+  const std::vector<Phase> st = make_steps(h->an, transpose != 0);
+  if (nsteps) *nsteps = (int)st.size();
+  for (int q = 0; q < (int)st.size() && q < cap && steps; ++q) {
+    const Phase &P = st[q];
     // every step starts at a slice edge and ends with a grid barrier, a CTA
     // barrier when it and the next step run on CTA 0 alone, or none when
     // both are small (staged: the next step waits for the values it reads)

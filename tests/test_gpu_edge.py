@@ -45,8 +45,22 @@ def star(nb, seed=0):
                        b=rng.standard_normal(3 * nb), cell_of_row=np.arange(nb), grid=(nb, 1, 1))
 
 
+def dense(nb, seed=0):
+    """Every block row coupled to every other: greedy coloring gives nb colors
+    (more than the single-launch apply takes: one launch per color step)."""
+    rng = np.random.default_rng(seed)
+    rowptr = (np.arange(nb + 1) * nb).astype(np.int32)
+    colind = np.tile(np.arange(nb, dtype=np.int32), nb)
+    vals = 0.05 * rng.standard_normal((nb * nb, 3, 3))
+    for i in range(nb):
+        vals[i * nb + i] += (2.0 + 0.1 * nb) * np.eye(3)
+    return BlockSystem(nb=nb, rowptr=rowptr, colind=colind, vals=vals,
+                       b=rng.standard_normal(3 * nb), cell_of_row=np.arange(nb), grid=(nb, 1, 1))
+
+
 CASES = {
     "one_row": lambda: generate(1, 1, 1, seed=0),
+    "dense_50_colors": lambda: dense(50, seed=4),
     "block_diagonal": lambda: block_diagonal(50, seed=1),
     "chain": lambda: generate(40, 1, 1, sigma=1.0, seed=2),
     "star": lambda: star(33, seed=3),

@@ -13,7 +13,19 @@ import scipy.sparse as sp
 from fpga_gb300 import GbIlu
 from fpga_gb300.synth import generate, make_config
 
+def _dense(nb):
+    """Every block row coupled to every other: nb colors, more steps than the
+    single-launch apply's fixed list holds (the per-step path)."""
+    from fpga_gb300.synth import BlockSystem
+    rowptr = (np.arange(nb + 1) * nb).astype(np.int32)
+    colind = np.tile(np.arange(nb, dtype=np.int32), nb)
+    vals = np.zeros((nb * nb, 3, 3))
+    return BlockSystem(nb=nb, rowptr=rowptr, colind=colind, vals=vals, b=np.zeros(3 * nb),
+                       cell_of_row=np.arange(nb), grid=(nb, 1, 1))
+
+
 CASES = {
+    "dense60": lambda: _dense(60),
     "c1": lambda: make_config("c1_20x20x10"),
     "faults": lambda: generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7),
     "mid": lambda: generate(60, 60, 20, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=5),
