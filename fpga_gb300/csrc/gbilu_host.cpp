@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <numeric>
 
 namespace gbilu {
@@ -31,6 +32,9 @@ int color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
 
 std::string check_pattern(int nb, const int *rowptr, const int *colind) {
   if (nb <= 0) return "nb must be positive";
+  // vector entries are indexed with int (3 per block row, 9 per block in
+  // per-row scratch)
+  if (nb > std::numeric_limits<int>::max() / 9) return "nb too large";
   if (!rowptr || !colind) return "rowptr/colind must not be NULL";
   if (rowptr[0] != 0) return "rowptr[0] must be 0";
   for (int i = 0; i < nb; ++i) {
