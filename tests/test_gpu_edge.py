@@ -58,8 +58,29 @@ def dense(nb, seed=0):
                        b=rng.standard_normal(3 * nb), cell_of_row=np.arange(nb), grid=(nb, 1, 1))
 
 
+def random_pattern(nb, p, seed):
+    """A random symmetric pattern (density p) with diagonally dominant random
+    blocks: color counts from a few to dozens."""
+    rng = np.random.default_rng(seed)
+    m = rng.random((nb, nb)) < p
+    m = m | m.T | np.eye(nb, dtype=bool)
+    rows, cols = np.nonzero(m)
+    rowptr = np.zeros(nb + 1, np.int32)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    vals = 0.1 * rng.standard_normal((len(cols), 3, 3))
+    deg = np.diff(rowptr)
+    for i in range(nb):
+        k = rowptr[i] + int(np.searchsorted(cols[rowptr[i]:rowptr[i + 1]], i))
+        vals[k] += (1.0 + 0.5 * deg[i]) * np.eye(3)
+    return BlockSystem(nb=nb, rowptr=rowptr, colind=cols.astype(np.int32), vals=vals,
+                       b=rng.standard_normal(3 * nb), cell_of_row=np.arange(nb), grid=(nb, 1, 1))
+
+
 CASES = {
     "one_row": lambda: generate(1, 1, 1, seed=0),
+    "random_sparse": lambda: random_pattern(400, 0.01, seed=5),
+    "random_mid": lambda: random_pattern(300, 0.08, seed=6),
     "dense_50_colors": lambda: dense(50, seed=4),
     "block_diagonal": lambda: block_diagonal(50, seed=1),
     "chain": lambda: generate(40, 1, 1, sigma=1.0, seed=2),

@@ -24,8 +24,27 @@ def _dense(nb):
                        cell_of_row=np.arange(nb), grid=(nb, 1, 1))
 
 
+def _random_pattern(seed):
+    """A random symmetric block pattern with its diagonal: from sparse chains
+    to dense clusters (many colors)."""
+    from fpga_gb300.synth import BlockSystem
+    rng = np.random.default_rng(seed)
+    nb = int(rng.integers(1, 160))
+    p = float(rng.choice([0.0, 0.01, 0.05, 0.3, 0.9]))
+    m = rng.random((nb, nb)) < p
+    m = m | m.T | np.eye(nb, dtype=bool)
+    rows, cols = np.nonzero(m)
+    rowptr = np.zeros(nb + 1, np.int32)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr).astype(np.int32)
+    return BlockSystem(nb=nb, rowptr=rowptr, colind=cols.astype(np.int32),
+                       vals=np.zeros((len(cols), 3, 3)), b=np.zeros(3 * nb),
+                       cell_of_row=np.arange(nb), grid=(nb, 1, 1))
+
+
 CASES = {
     "dense60": lambda: _dense(60),
+    **{f"random{k}": (lambda k=k: _random_pattern(k)) for k in range(12)},
     "c1": lambda: make_config("c1_20x20x10"),
     "faults": lambda: generate(30, 24, 12, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=7),
     "mid": lambda: generate(60, 60, 20, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=5),
