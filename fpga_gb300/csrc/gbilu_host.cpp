@@ -49,6 +49,18 @@ std::string check_pattern(int nb, const int *rowptr, const int *colind) {
     }
     if (!diag) return "missing diagonal block in row " + std::to_string(i);
   }
+  // Structural symmetry (block (i, j) present iff (j, i) is), as in the
+  // simulator's matrices: rows of one color must not be coupled in either
+  // direction, and the coloring only sees each row's own columns.
+  for (int i = 0; i < nb; ++i)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = colind[k];
+      if (j == i) continue;
+      if (!std::binary_search(colind + rowptr[j], colind + rowptr[j + 1], i))
+        return "pattern must be structurally symmetric: block (" + std::to_string(i) + ", " +
+               std::to_string(j) + ") has no transpose (" + std::to_string(j) + ", " +
+               std::to_string(i) + ")";
+    }
   return "";
 }
 

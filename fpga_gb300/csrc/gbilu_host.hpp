@@ -64,7 +64,7 @@ struct Analysis {
 int color_greedy(int nb, const int *rowptr, const int *colind, int *color);
 
 // Validates the pattern (sorted unique columns, diagonal present, indices in
-// range); returns an empty string when it is fine.
+// range, structurally symmetric); returns an empty string when it is fine.
 std::string check_pattern(int nb, const int *rowptr, const int *colind);
 
 // Builds everything above from an input pattern. Returns "" or an error.

@@ -150,7 +150,9 @@ int gbilu_destroy(void *handle);
 
 /* Sparsity analysis: greedy block coloring, color-ordered permutation,
  * L/U split and the device layout. rowptr[nb+1], colind[nnzb] 0-based,
- * columns sorted and unique per row, diagonal block present.
+ * columns sorted and unique per row, diagonal block present, the pattern
+ * structurally symmetric (block (i, j) present iff (j, i) is, as in the
+ * simulator's matrices; values need not be symmetric).
  * Structure of fpga_setup_host_datamem's sizes (fpga_functions_bicgstab.cpp
  * :84-131) and of the coloring that fills vectorPointers (:608-629). */
 int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind);

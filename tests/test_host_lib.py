@@ -70,6 +70,14 @@ def test_error_behaviour(built_lib):
         keep[np.nonzero(s.colind[s.rowptr[3]:s.rowptr[4]] == 3)[0][0] + s.rowptr[3]] = False
         rp = np.concatenate([[0], np.cumsum([keep[s.rowptr[i]:s.rowptr[i + 1]].sum() for i in range(s.nb)])])
         expect(native.BAD_INPUT, g.analyze, rp, s.colind[keep])
+        # a structurally nonsymmetric pattern: row 3 loses one off-diagonal
+        # block whose transpose stays
+        keep = np.ones(s.nnzb, bool)
+        off = [k for k in range(s.rowptr[3], s.rowptr[4]) if s.colind[k] != 3]
+        keep[off[0]] = False
+        rp = np.concatenate([[0], np.cumsum([keep[s.rowptr[i]:s.rowptr[i + 1]].sum() for i in range(s.nb)])])
+        with pytest.raises(GbIluError, match="structurally symmetric"):
+            g.analyze(rp.astype(np.int32), s.colind[keep])
         g.analyze(s.rowptr, s.colind)
         vals = s.vals.copy()
         d = np.nonzero(s.colind[s.rowptr[10]:s.rowptr[11]] == 10)[0][0] + s.rowptr[10]
