@@ -83,8 +83,9 @@ struct Handle {
   cudaStream_t st = nullptr, cap = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   // host-buffer solves move b on aux while the initial SpMV runs on st
+  // (e_x: x0 is on the device; e_b: b is)
   cudaStream_t aux = nullptr;
-  cudaEvent_t e_b = nullptr;
+  cudaEvent_t e_x = nullptr, e_b = nullptr;
   DevBuf<int2> srows;
   // perm/iperm: device row <-> input row (the vectors of a solve);
   // fperm: permuted row -> input row (the pattern-ordered gradient);
@@ -599,6 +600,7 @@ int setup_device(Handle *h) {
     CK(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->e_x, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&h->e_b, cudaEventDisableTiming));
     CK(cudaEventCreate(&h->e0));
     CK(cudaEventCreate(&h->e1));
@@ -748,10 +750,11 @@ int check_solve_ready(Handle *h) {
 // FP64 BiCGSTAB on the permuted vectors: b in h->b64, x in v64.x.
 // With sync false the final Ctl is only queued for copy into h->h_ctl: the
 // caller synchronizes once at the end (no host round trip mid-solve).
-// b_ready: an event after which b64 holds b (b is moved on another stream
-// while A x0 is computed), or null when b64 is ready in stream order.
+// b_ready: an event after which b is on the device (it is moved on another
+// stream while A x0 is computed), or null when it is ready in stream order.
+// b_in: b in the input numbering (permuted as it is read), or null for b64.
 int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long long &launches,
-            bool sync = true, cudaEvent_t b_ready = nullptr) {
+            bool sync = true, cudaEvent_t b_ready = nullptr, const double *b_in = nullptr) {
   const int n = 3 * h->an.nb;
   Ops<double, double> o = make_ops<double, double>(h, transpose);
   Vecs<double> &w = h->v64;
@@ -762,7 +765,8 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   launches += l;
   if (b_ready) CK(cudaStreamWaitEvent(h->st, b_ready, 0));
   k_init_resid<double><<<reduce_grid(h, n), kThreads, 0, h->st>>>(
-      h->ctl.p, n, h->b64.p, w.r.p, w.rt.p, w.p.p, h->partials.p);
+      h->ctl.p, n, b_in ? b_in : h->b64.p, b_in ? h->perm.p : nullptr, w.r.p, w.rt.p, w.p.p,
+      h->partials.p);
   launches += 1;
   int rc = run_loop<double, double>(h, transpose, maxit, launches);
   if (rc) return rc;
@@ -957,6 +961,7 @@ int gbilu_destroy(void *handle) {
     cudaStreamDestroy(h->st);
     cudaStreamDestroy(h->cap);
     cudaStreamDestroy(h->aux);
+    cudaEventDestroy(h->e_x);
     cudaEventDestroy(h->e_b);
     cudaEventDestroy(h->e0);
     cudaEventDestroy(h->e1);
@@ -1092,25 +1097,35 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
     }
   }
   // The FP64 solve needs b only after A x0 (k_init_resid): from host
-  // buffers, b moves on the auxiliary stream while the SpMV runs.
+  // buffers, b moves on the auxiliary stream while the SpMV runs. The
+  // CPU-GPU link is one shared budget (about 200 GB/s for reads and writes
+  // together, measured), so x0 goes first and alone; b follows on the copy
+  // engine, which takes no SMs from the SpMV, and is permuted on the device.
   const bool fp64 = h->opt.precision != GBILU_MIXED;
   const bool overlap_b = fp64 && !device_ptrs;
-  cudaStream_t sb = overlap_b ? h->aux : h->st;
-  if (overlap_b) CK(cudaStreamWaitEvent(h->aux, h->e0, 0));
-  if (!device_ptrs && !mapped_x) {
-    CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, sb));
+  if (!device_ptrs && !mapped_x)
     CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-  }
-  if (mapped_x) {
-    // host side read in order, device side written permuted
-    k_scatter<double><<<g, kThreads, 0, sb>>>(nb, h->iperm.p, db, h->b64.p);
+  if (mapped_x)   // host side read in order, device side written permuted
     k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, dx, h->v64.x.p);
-  } else {
-    k_gather<double, double><<<g, kThreads, 0, sb>>>(nb, h->perm.p, db, h->b64.p, 1.0);
+  else
     k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
+  cudaStream_t sb = h->st;
+  if (overlap_b) {
+    CK(cudaEventRecord(h->e_x, h->st));
+    CK(cudaStreamWaitEvent(h->aux, h->e_x, 0));
+    sb = h->aux;
   }
-  if (overlap_b) CK(cudaEventRecord(h->e_b, h->aux));
-  launches += 2;
+  if (!device_ptrs && (!mapped_x || overlap_b)) {
+    CK(cudaMemcpyAsync(h->io64.p, b, n * sizeof(double), cudaMemcpyHostToDevice, sb));
+    db = h->io64.p;
+  }
+  if (overlap_b)   // k_init_resid permutes b as it reads it
+    CK(cudaEventRecord(h->e_b, h->aux));
+  else if (mapped_x)
+    k_scatter<double><<<g, kThreads, 0, sb>>>(nb, h->iperm.p, db, h->b64.p);
+  else
+    k_gather<double, double><<<g, kThreads, 0, sb>>>(nb, h->perm.p, db, h->b64.p, 1.0);
+  launches += overlap_b ? 1 : 2;
   Ctl c;
   gbilu_result tmp;
   memset(&tmp, 0, sizeof tmp);
@@ -1119,7 +1134,8 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   if (!fp64)
     rc = solve_mixed(h, transpose, tol, maxit, r, c, launches);
   else
-    rc = solve64(h, transpose, tol, maxit, c, launches, false, overlap_b ? h->e_b : nullptr);
+    rc = solve64(h, transpose, tol, maxit, c, launches, false, overlap_b ? h->e_b : nullptr,
+                 overlap_b ? db : nullptr);
   if (rc) return rc;
   // x back to the caller's numbering. When the initial residual already met
   // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged

@@ -1030,15 +1030,17 @@ __global__ void k_wait_probe(Ctl *ctl, int mode, const double *word) {
 // Steps 0/1 of the FP64 solve after y = A x0 (k_spmv PLAIN into r):
 // r = b - y (the RESID epilogue's arithmetic), rt = p = r, rho = ||r||^2 and
 // the stop tests of the start. Split from the SpMV so that b can still be in
-// transit while A x0 is computed.
+// transit while A x0 is computed. perm non-null: b is in the input numbering
+// (device row i reads input row perm[i], as k_gather).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-k_init_resid(Ctl *ctl, int n, const T *__restrict__ b, T *__restrict__ r, T *__restrict__ rt,
-             T *__restrict__ p, double *partials) {
+k_init_resid(Ctl *ctl, int n, const T *__restrict__ b, const int *__restrict__ perm,
+             T *__restrict__ r, T *__restrict__ rt, T *__restrict__ p, double *partials) {
   double d = 0.0;
   DF f = {0.f, 0.f};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const T v = b[i] - r[i];
+    const int row = i / 3;
+    const T v = (perm ? b[3 * perm[row] + (i - 3 * row)] : b[i]) - r[i];
     r[i] = v; rt[i] = v; p[i] = v;
     if (sizeof(T) == 8) d += (double)v * v; else df_add_prod(f, (float)v, (float)v);
   }
