@@ -78,6 +78,13 @@ def test_error_behaviour(built_lib):
         rp = np.concatenate([[0], np.cumsum([keep[s.rowptr[i]:s.rowptr[i + 1]].sum() for i in range(s.nb)])])
         with pytest.raises(GbIluError, match="structurally symmetric"):
             g.analyze(rp.astype(np.int32), s.colind[keep])
+        # empty system; a block-row count whose vector indices overflow int
+        # (rejected before the arrays are read)
+        with pytest.raises(GbIluError, match="nb must be positive"):
+            g.analyze(np.zeros(1, np.int32), np.zeros(0, np.int32))
+        rp1, ci1 = np.zeros(2, np.int32), np.zeros(1, np.int32)
+        assert g.L.gbilu_analyze(g.h, 2**31 // 9 + 1, rp1, ci1) == native.BAD_INPUT
+        assert "nb too large" in g.L.gbilu_last_error(g.h).decode()
         g.analyze(s.rowptr, s.colind)
         vals = s.vals.copy()
         d = np.nonzero(s.colind[s.rowptr[10]:s.rowptr[11]] == 10)[0][0] + s.rowptr[10]
