@@ -204,8 +204,33 @@ def test_pinned_host_buffers_bit_identical(case):
         r2 = g.solve_host_ptr(b.data_ptr(), x.data_ptr(), 1e-6, 500)
         assert r1.status == r2.status and r1.half_iters == r2.half_iters
         assert np.array_equal(x.numpy(), x1)
+        x3 = x0_np.copy()      # page-locked b, ordinary x: staging copies
+        r3 = g.solve_host_ptr(b.data_ptr(), x3.ctypes.data, 1e-6, 500)
+        assert r3.half_iters == r1.half_iters and np.array_equal(x3, x1)
         if r1.status == 2:
             assert np.array_equal(x1, x0_np)
+
+
+def test_pinned_host_buffers_mixed_bit_identical(case):
+    """The mixed form reads b and x0 before its first FP64 residual: from
+    page-locked buffers in place, from ordinary memory through staging
+    copies; the same bits either way, and the same as device pointers."""
+    torch = pytest.importorskip("torch")
+    s, P, _ = case
+    x0 = np.random.default_rng(4).standard_normal(s.n)
+    with GbIlu(device=0, precision="mixed") as g:
+        g.analyze(s.rowptr, s.colind).factor(s.vals)
+        for x0_np in (np.zeros(s.n), x0):
+            x1 = x0_np.copy()
+            r1 = g.solve_host_ptr(s.b.ctypes.data, x1.ctypes.data, 1e-8, 500)
+            b = torch.from_numpy(s.b.copy()).pin_memory()
+            x = torch.from_numpy(x0_np.copy()).pin_memory()
+            r2 = g.solve_host_ptr(b.data_ptr(), x.data_ptr(), 1e-8, 500)
+            bd, xd = b.cuda(), torch.from_numpy(x0_np.copy()).cuda()
+            r3 = g.solve_device(bd.data_ptr(), xd.data_ptr(), 1e-8, 500)
+            assert r1.status == r2.status == r3.status == 0
+            assert r1.outer_iters == r2.outer_iters == r3.outer_iters
+            assert np.array_equal(x.numpy(), x1) and np.array_equal(xd.cpu().numpy(), x1)
 
 
 def test_deterministic(case):
