@@ -204,7 +204,7 @@ def gpu_bench(args, world, rank, local):
     # e2e: host pinned buffers through gbilu_solve (H2D b, x0; D2H x inside)
     b_pin = torch.from_numpy(s.b).pin_memory()
     x_pin = torch.zeros(n, dtype=torch.float64).pin_memory()
-    for _ in range(2):
+    for _ in range(max(2, args.warmup)):
         x_pin.zero_()
         g64.solve_host_ptr(b_pin.data_ptr(), x_pin.data_ptr(), tol, maxit)
     e2e_ms = []
