@@ -198,7 +198,11 @@ int gbilu_get_factors(void *handle, double *lu, double *dinv);
 /* Solve A x = b. b[3*nb] and x[3*nb] are HOST arrays in the original
  * numbering; x holds x0 on entry and the solution on return. tol and maxit
  * follow the reference: maxit full iterations plus the first half of one
- * more (solver.vhd:557, solver_pkg.vhd:127-128). res may be NULL. */
+ * more (solver.vhd:557, solver_pkg.vhd:127-128). res may be NULL.
+ * When both arrays are page-locked (cudaHostAlloc / cudaHostRegister), x0
+ * and x move over the CPU-GPU link in place and b by the copy engine while
+ * A x0 is computed; other host memory goes through staging copies. Both
+ * give the same bits. */
 int gbilu_solve(void *handle, const double *b, double *x, double tol,
                 int maxit, gbilu_result *res);
 
