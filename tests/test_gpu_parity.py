@@ -207,6 +207,11 @@ def test_pinned_host_buffers_bit_identical(case):
         x3 = x0_np.copy()      # page-locked b, ordinary x: staging copies
         r3 = g.solve_host_ptr(b.data_ptr(), x3.ctypes.data, 1e-6, 500)
         assert r3.half_iters == r1.half_iters and np.array_equal(x3, x1)
+        # device arrays: b permuted by its own kernel instead of inside the
+        # initial-residual kernel
+        bd, xd = b.cuda(), torch.from_numpy(x0_np.copy()).cuda()
+        r4 = g.solve_device(bd.data_ptr(), xd.data_ptr(), 1e-6, 500)
+        assert r4.half_iters == r1.half_iters and np.array_equal(xd.cpu().numpy(), x1)
         if r1.status == 2:
             assert np.array_equal(x1, x0_np)
 
