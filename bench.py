@@ -14,8 +14,10 @@ reference has no CPU solver; its arithmetic exists only as FPGA RTL) on all
 host cores.
 
 Multi-GPU: the solve does not shard without changing the preconditioner, so
-N > 1 runs N independent replicas (one system per rank, seeded by rank),
-value = max-over-ranks time / (K * N).
+N > 1 runs N independent replicas (one system per rank, seeded by rank):
+value = the max over ranks of the per-solve device time (weak scaling: the
+work per GPU is fixed), and ``replicas.solves_per_s`` the aggregate
+throughput of all ranks.
 """
 from __future__ import annotations
 
@@ -121,6 +123,29 @@ def barrier(world):
         dist.barrier()
 
 
+def workload_config(s, cfg, nnzb, ncolors, world):
+    """The config dict both arms print (same keys, same workload)."""
+    return {"workload": WORKLOAD, "grid": list(cfg["grid"]), "nb": s.nb, "nnzb": nnzb,
+            "colors": ncolors, "tol": cfg["tol"], "sigma": cfg["sigma"],
+            "inactive": cfg["inactive"], "faults": cfg["faults"], "x0": "zero",
+            "l2": "inputs larger than L2 (FP64 A 0.23 GB, L+U 0.19 GB)",
+            "parallelism": f"replicas{world}" if world > 1 else "single"}
+
+
+def host_cpu():
+    """CPU model and thread count of the host running the CPU legs."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    return {"model": model, "nproc": os.cpu_count()}
+
+
 def cpu_reference(args, world, rank):
     """The reference arm: the CPU restatement (oracle) on all host cores."""
     if rank != 0:
@@ -132,7 +157,8 @@ def cpu_reference(args, world, rank):
     cores = os.cpu_count() or 1
     s = make_config(WORKLOAD)
     P = Prepared(s)
-    tol = CONFIGS[WORKLOAD]["tol"]
+    cfg = CONFIGS[WORKLOAD]
+    tol = cfg["tol"]
     for _ in range(max(1, args.warmup)):
         P.solve_omp(s.b, tol=tol, maxit=1000, nthreads=cores)
     times = []
@@ -145,9 +171,10 @@ def cpu_reference(args, world, rank):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded generator, no dataset)",
-           "config": {"workload": WORKLOAD, "grid": [100, 100, 50], "nb": s.nb, "tol": tol,
-                      "half_iters": r.half_iters, "relres": r.relres},
+           "config": workload_config(s, cfg, s.nnzb, P.ncolors, world),
+           "result": {"status": r.status, "half_iters": r.half_iters, "relres": r.relres},
            "cpu_baseline": {"value": ms, "unit": "ms", "cores": cores, "kind": "port",
+                            "cpu": host_cpu(),
                             "sample": f"{args.steps} full solves of {WORKLOAD} to relres {tol} "
                                       "(OpenMP C restatement of the reference algorithm)"},
            "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -195,8 +222,10 @@ def gpu_bench(args, world, rank, local):
         barrier(world)
     clocks = clk.summary()
     # device time of the solves (CUDA events on the library's stream), max over ranks
+    # weak scaling: every rank solves its own system; the value is the
+    # slowest rank's per-solve time, the aggregate rate is reported beside it
     ms_step = barrier_max(world, dev_ms / args.steps)
-    value = ms_step / world
+    value = ms_step
     r0 = res[-1]
     x_np = x_dev.cpu().numpy()
     true_relres = float(np.linalg.norm(s.b - s.to_scipy() @ x_np) / np.linalg.norm(s.b))
@@ -213,7 +242,7 @@ def gpu_bench(args, world, rank, local):
         t0 = time.perf_counter()
         g64.solve_host_ptr(b_pin.data_ptr(), x_pin.data_ptr(), tol, maxit)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e = barrier_max(world, statistics.mean(e2e_ms)) / world
+    e2e = barrier_max(world, statistics.mean(e2e_ms))
 
     # dominant-kernel roofline: kernels timed back to back with CUDA events
     peak, peak_kind = peaks()
@@ -257,12 +286,8 @@ def gpu_bench(args, world, rank, local):
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                "dtype": "f64", "data": "synthetic (seeded generator, no dataset)",
-               "config": {"workload": WORKLOAD, "grid": [100, 100, 50], "nb": s.nb,
-                          "nnzb": st["nnzb"], "colors": st["ncolors"], "tol": tol,
-                          "sigma": cfg["sigma"], "inactive": cfg["inactive"],
-                          "faults": cfg["faults"], "x0": "zero",
-                          "l2": "inputs larger than L2 (FP64 A 0.23 GB, L+U 0.19 GB)",
-                          "parallelism": f"replicas{world}" if world > 1 else "single"},
+               "config": workload_config(s, cfg, st["nnzb"], st["ncolors"], world),
+               "replicas": {"ranks": world, "solves_per_s": world * 1e3 / ms_step},
                "result": {"status": r0.status, "half_iters": r0.half_iters,
                           "relres": r0.relres, "true_relres": true_relres},
                "wall_ms_per_step": wall_ms / args.steps,
@@ -282,21 +307,49 @@ def gpu_bench(args, world, rank, local):
 
 
 def cpu_baseline(s, tol, maxit):
-    """The oracle's OpenMP solver on the host cores, a bounded sample."""
+    """The oracle's OpenMP solver on the host cores, bounded samples: the
+    headline system at its tolerance (the line's cpu_baseline) and, under
+    ``others``, the other workloads and tolerances the GPU numbers are
+    quoted on (median of 3 solves each, after one warm-up)."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Prepared
+    from fpga_gb300.synth import make_config, CONFIGS
     cores = os.cpu_count() or 1
+
+    def timed(P, b, t, m, reps):
+        P.solve_omp(b, tol=t, maxit=m, nthreads=cores)
+        times = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            x, r = P.solve_omp(b, tol=t, maxit=m, nthreads=cores)
+            times.append((time.perf_counter() - t0) * 1e3)
+        return statistics.median(times), r
+
     P = Prepared(s)
-    P.solve_omp(s.b, tol=tol, maxit=maxit, nthreads=cores)
     times = []
+    P.solve_omp(s.b, tol=tol, maxit=maxit, nthreads=cores)
     t_end = time.perf_counter() + 10.0
     while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 20):
         t0 = time.perf_counter()
         P.solve_omp(s.b, tol=tol, maxit=maxit, nthreads=cores)
         times.append((time.perf_counter() - t0) * 1e3)
-    return {"value": statistics.median(times), "unit": "ms", "cores": cores, "kind": "port",
-            "sample": f"{len(times)} full solves of {WORKLOAD} to relres {tol} "
-                      "(median; OpenMP C restatement, oracle/gbilu_oracle.c)"}
+    out = {"value": statistics.median(times), "unit": "ms", "cores": cores, "kind": "port",
+           "cpu": host_cpu(),
+           "sample": f"{len(times)} full solves of {WORKLOAD} to relres {tol} "
+                     "(median; OpenMP C restatement, oracle/gbilu_oracle.c)"}
+    others = []
+    ms, r = timed(P, s.b, 1e-6, maxit, 3)
+    others.append({"workload": WORKLOAD, "form": "fp64", "tol": 1e-6, "ms": ms,
+                   "half_iters": r.half_iters})
+    for wl, t in (("c1_20x20x10", 1e-2), ("c3_100x100x50_mixed", 1e-8),
+                  ("c4_60x60x30_adjoint", 1e-10)):
+        s2 = make_config(wl)
+        P2 = Prepared(s2)
+        ms, r = timed(P2, s2.b, t, CONFIGS[wl]["maxit"], 3)
+        others.append({"workload": wl, "form": "fp64 forward", "tol": t, "ms": ms,
+                       "half_iters": r.half_iters})
+    out["others"] = others
+    return out
 
 
 def secondary(args, local, tol64):
@@ -323,6 +376,12 @@ def secondary(args, local, tol64):
         g.close()
     A = s.to_scipy()
     err = float(np.linalg.norm(sols["mixed"] - sols["fp64"]) / np.linalg.norm(sols["fp64"]))
+    # against the CPU oracle's FP64 solve to the same tolerance (the checker)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle_lib import Prepared
+    x_orc, r_orc = Prepared(s).solve_omp(s.b, tol=tol, maxit=c3["maxit"],
+                                         nthreads=os.cpu_count() or 1)
+    err_orc = {p: float(np.linalg.norm(sols[p] - x_orc) / np.linalg.norm(x_orc)) for p in sols}
     tr = {p: float(np.linalg.norm(s.b - A @ sols[p]) / np.linalg.norm(s.b)) for p in sols}
     out["mixed"] = {"workload": "c3_100x100x50_mixed (sigma=2.0)", "tol": tol,
                     "fp64_ms": times["fp64"][0], "mixed_ms": times["mixed"][0],
@@ -330,7 +389,10 @@ def secondary(args, local, tol64):
                     "fp64_half_iters": times["fp64"][1].half_iters,
                     "mixed_outer": times["mixed"][1].outer_iters,
                     "mixed_inner_half_iters": times["mixed"][1].inner_half_iters,
-                    "true_relres": tr, "x_err_vs_fp64": err}
+                    "true_relres": tr, "x_err_vs_fp64": err,
+                    "x_err_vs_oracle": err_orc["mixed"],
+                    "fp64_x_err_vs_oracle": err_orc["fp64"],
+                    "oracle_half_iters": r_orc.half_iters}
     # the 4,000-cell system at 1e-2 and the 500k-cell one at 1e-2 and 1e-6,
     # FP64 and mixed
     rows = []
@@ -354,27 +416,46 @@ def secondary(args, local, tol64):
                                                   np.linalg.norm(s2.b))})
             g.close()
     out["tolerances"] = rows
-    # adjoint / forward on the 60x60x30 system
+    # adjoint / forward on the 60x60x30 system, device arrays: the forward
+    # solve against the transposed solve alone and against the whole
+    # backward pass (transposed solve, gathers and dL/dA on the pattern)
+    import torch
     c4 = CONFIGS["c4_60x60x30_adjoint"]
     s = make_config("c4_60x60x30_adjoint")
     g = GbIlu(device=local, precision="fp64")
     g.analyze(s.rowptr, s.colind).factor(s.vals)
     cells, d = adjoint_selection(s.nb)
     idx = (3 * cells[:, None] + np.arange(3)).reshape(-1)
-    x, r = g.solve(s.b, tol=c4["tol"], maxit=c4["maxit"])
-    fw, bw = [], []
-    for _ in range(3):
-        t0 = time.perf_counter()
-        x, r = g.solve(s.b, tol=c4["tol"], maxit=c4["maxit"])
-        fw.append(r.device_ms)
+    dev = torch.device(f"cuda:{local}")
+    bd = torch.from_numpy(s.b).to(dev)
+    xd = torch.zeros(s.n, dtype=torch.float64, device=dev)
+    ld = torch.zeros(s.n, dtype=torch.float64, device=dev)
+    dAd = torch.zeros(s.nnzb * 9, dtype=torch.float64, device=dev)
+    fw, bw, bw_full = [], [], []
+    for rep in range(4):
+        xd.zero_()
+        r = g.solve_device(bd.data_ptr(), xd.data_ptr(), tol=c4["tol"], maxit=c4["maxit"])
+        x = xd.cpu().numpy()
         gvec = np.zeros(s.n)
         gvec[idx] = x[idx] - d
-        lam, dA, ra = g.adjoint(gvec, x, tol=c4["tol"], maxit=c4["maxit"])
-        bw.append(ra.device_ms)
+        gd = torch.from_numpy(gvec).to(dev)
+        ra = g.adjoint_device(gd.data_ptr(), xd.data_ptr(), ld.data_ptr(), None,
+                              tol=c4["tol"], maxit=c4["maxit"])
+        rf = g.adjoint_device(gd.data_ptr(), xd.data_ptr(), ld.data_ptr(), dAd.data_ptr(),
+                              tol=c4["tol"], maxit=c4["maxit"])
+        if rep:   # the first round is the warm-up
+            fw.append(r.device_ms)
+            bw.append(ra.device_ms)
+            bw_full.append(rf.device_ms)
+    f_ms = statistics.median(fw)
     out["adjoint"] = {"workload": "c4_60x60x30_adjoint", "tol": c4["tol"],
-                      "forward_ms": statistics.median(fw), "adjoint_ms": statistics.median(bw),
-                      "ratio": statistics.median(bw) / statistics.median(fw),
-                      "forward_half_iters": r.half_iters, "adjoint_half_iters": ra.half_iters}
+                      "forward_ms": f_ms, "adjoint_ms": statistics.median(bw),
+                      "adjoint_ms_full": statistics.median(bw_full),
+                      "ratio": statistics.median(bw) / f_ms,
+                      "ratio_full": statistics.median(bw_full) / f_ms,
+                      "forward_half_iters": r.half_iters, "adjoint_half_iters": rf.half_iters,
+                      "timing": "device arrays, CUDA events; full = transposed solve + "
+                                "gathers + dL/dA (nnzb*9 doubles written)"}
     g.close()
     out["adjoint_mixed_2m"] = mixed_adjoint_2m(local)
     return out
@@ -398,15 +479,22 @@ def mixed_adjoint_2m(local):
         free0, total = torch.cuda.mem_get_info(local)
         g = GbIlu(device=local, precision=prec)
         g.analyze(s.rowptr, s.colind).factor(s.vals)
-        x, r = g.solve(s.b, tol=c5["tol"], maxit=c5["maxit"])
+        # the first forward and adjoint build their graphs: timed second
+        for rep in range(2):
+            x, r = g.solve(s.b, tol=c5["tol"], maxit=c5["maxit"])
         gv = np.zeros(s.n)
         gv[idx] = x[idx] - d
-        lam, dA, ra = g.adjoint(gv, x, tol=c5["tol"], maxit=c5["maxit"])
+        for rep in range(2):
+            lam, dA, ra = g.adjoint(gv, x, tol=c5["tol"], maxit=c5["maxit"])
+        _, _, ra0 = g.adjoint(gv, x, tol=c5["tol"], maxit=c5["maxit"], want_dA=False)
         free1, _ = torch.cuda.mem_get_info(local)
         fw = r.device_ms
-        bw = ra.device_ms
+        bw, bw_full = ra0.device_ms, ra.device_ms
         grads[prec] = (lam, dA)
+        # host arrays: device_ms of each includes its host<->device copies
+        # inside the timed region (b and x0; g, and x for dL/dA)
         res[prec] = {"forward_ms": fw, "adjoint_ms": bw, "ratio": bw / fw,
+                     "adjoint_ms_full": bw_full, "ratio_full": bw_full / fw,
                      "forward_status": r.status, "adjoint_status": ra.status,
                      "forward_true_relres": r.true_relres, "adjoint_true_relres": ra.true_relres,
                      "device_bytes_handle": g.stats()["device_bytes"],

@@ -89,8 +89,9 @@ struct Handle {
   DevBuf<int2> srows;
   // perm/iperm: device row <-> input row (the vectors of a solve);
   // fperm: permuted row -> input row (the pattern-ordered gradient);
-  // dperm: device row -> permuted row (the device factorization's layout)
-  DevBuf<int> perm, iperm, fperm, dperm, prowptr, pcol, psrc;
+  // dperm: device row -> permuted row (the device factorization's layout);
+  // pdev: permuted row -> device row (the gradient's gather of lambda)
+  DevBuf<int> perm, iperm, fperm, dperm, pdev, prowptr, pcol, psrc;
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
   DevBuf<float> dinv32, dinvT32;
@@ -584,6 +585,7 @@ void release_device(Handle *h) {
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
   h->srows.release(); h->perm.release(); h->iperm.release(); h->fperm.release(); h->dperm.release();
+  h->pdev.release();
   h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
@@ -632,6 +634,8 @@ int setup_device(Handle *h) {
   CK(cudaMemcpy(h->fperm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->dperm.alloc(an.nb));
   CK(cudaMemcpy(h->dperm.p, an.dperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  CK(h->pdev.alloc(an.nb));
+  CK(cudaMemcpy(h->pdev.p, an.idperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->prowptr.alloc(an.nb + 1));
   CK(cudaMemcpy(h->prowptr.p, an.prowptr.data(), (an.nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->pcol.alloc(an.nnzb));
@@ -684,7 +688,7 @@ int setup_device(Handle *h) {
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
-                     (size_t)an.nnzb * 8 + (size_t)an.nb * 20;
+                     (size_t)an.nnzb * 8 + (size_t)an.nb * 24;
   return GBILU_OK;
 }
 
@@ -872,15 +876,21 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
   }
   const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
   int outer_steps = 0, inner_half = 0;
-  while (nrm > bound && outer_steps < h->opt.max_outer) {
+  // maxit caps the inner half-iterations of all refinement steps together
+  // the way the reference caps one run: at most maxit full iterations plus
+  // the first half of one more, 2*maxit + 1 halves (solver.vhd:557). Each
+  // inner solve gets the full iterations that still fit.
+  const long long budget = 2LL * maxit + 1;
+  while (nrm > bound && outer_steps < h->opt.max_outer && inner_half < budget) {
+    const int left = (int)std::min<long long>((budget - inner_half - 1) / 2, h->opt.inner_maxit);
     // right-hand side of the correction equation A d = r / ||r|| in FP32
     // (staged in f.t, which the inner run overwrites only after reading it)
     k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0 / nrm, w.r.p, f.t.p);
-    k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, h->opt.inner_tol, 0, h->opt.inner_maxit, tmo);
+    k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, h->opt.inner_tol, 0, left, tmo);
     k_init_rhs<float><<<reduce_grid(h, n), kThreads, 0, h->st>>>(h->ctl.p, n, f.t.p, f.r.p, f.rt.p,
                                                                  f.p.p, f.x.p, h->partials.p);
     launches += 3;
-    rc = run_loop<float, float>(h, transpose, h->opt.inner_maxit, launches);
+    rc = run_loop<float, float>(h, transpose, left, launches);
     if (rc) return rc;
     CK(cudaMemcpyAsync(h->h_ctl, h->ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -896,9 +906,9 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
     if (!std::isfinite(nrm)) { out.status = ST_NONFINITE; break; }
     if (ic.status == ST_TIMEOUT) { out.status = ST_TIMEOUT; break; }
   }
-  (void)maxit;
   if (nrm <= bound) out.status = ST_OK;
   out.norm = nrm;
+  // the counter of one run that did all inner halves back to back
   out.half = inner_half - 1;
   if (res) {
     res->outer_iters = outer_steps;
@@ -934,6 +944,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->mixed_scheme = 0;
   o->ru_delta = 0.1;
   o->stage_small_steps = 1;
+  o->coloring = 0;
   return GBILU_OK;
 }
 
@@ -976,7 +987,9 @@ int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind) {
   if (!h) return GBILU_BAD_INPUT;
   auto t0 = std::chrono::steady_clock::now();
   h->analyzed = h->factored = false;
-  std::string err = analyze(nb, rowptr, colind, h->an, true);
+  if (h->opt.coloring != 0 && h->opt.coloring != 1)
+    return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: coloring must be 0 or 1");
+  std::string err = analyze(nb, rowptr, colind, h->an, true, h->opt.coloring);
   if (!err.empty()) return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: %s", err.c_str());
   h->analyzed = true;
   if (h->opt.device >= 0) {
@@ -1062,8 +1075,14 @@ int gbilu_get_factors(void *handle, double *lu, double *dinv) {
   return GBILU_OK;
 }
 
+// One solve through the ABI. With gx and gdA (the adjoint), after the
+// transposed solve the gradient dL/dA = -lambda_i x_j^T is formed on the
+// device from lambda (still in the device vector) and gx (the forward
+// solution, input numbering), inside the timed region, into gdA (input
+// block order; host or device like the other arrays).
 static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, bool transpose,
-                      double tol, int maxit, gbilu_result *res) {
+                      double tol, int maxit, gbilu_result *res, const double *gx = nullptr,
+                      double *gdA = nullptr) {
   int rc = check_solve_ready(h);
   if (rc) return rc;
   if (!b || !x) return h->fail(GBILU_BAD_INPUT, "b and x must not be NULL");
@@ -1137,6 +1156,21 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
     rc = solve64(h, transpose, tol, maxit, c, launches, false, overlap_b ? h->e_b : nullptr,
                  overlap_b ? db : nullptr);
   if (rc) return rc;
+  if (gx && gdA) {
+    // lambda from the device numbering and x from the input numbering into
+    // the permuted numbering of the pattern arrays, then dL/dA
+    const double *xin = gx;
+    if (!device_ptrs) {   // b's staging buffer is free once the solve read it
+      CK(cudaMemcpyAsync(h->io64.p, gx, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      xin = h->io64.p;
+    }
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->pdev.p, h->v64.x.p, h->v64.r.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, xin, h->v64.s.p, 1.0);
+    k_grad_a<<<grid_for(h, nb), kThreads, 0, h->st>>>(nb, h->prowptr.p, h->pcol.p, h->psrc.p,
+                                                      h->v64.r.p, h->v64.s.p,
+                                                      device_ptrs ? gdA : h->dA.p);
+    launches += 3;
+  }
   // x back to the caller's numbering. When the initial residual already met
   // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged
   // bit for bit; the FP64 path therefore needs no status before it and the
@@ -1150,6 +1184,9 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   CK(cudaEventRecord(h->e1, h->st));
   if (!device_ptrs && !mapped_x)
     CK(cudaMemcpyAsync(x, h->io64b.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (gx && gdA && !device_ptrs)
+    CK(cudaMemcpyAsync(gdA, h->dA.p, (size_t)h->an.nnzb * 9 * sizeof(double),
+                       cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   CK(last_error(h));
   if (fp64) {
@@ -1237,26 +1274,29 @@ int gbilu_adjoint(void *handle, const double *g_in, const double *x, double *lam
   Handle *h = static_cast<Handle *>(handle);
   if (!h) return GBILU_BAD_INPUT;
   if (!g_in || !x || !lambda) return h->fail(GBILU_BAD_INPUT, "g, x and lambda must not be NULL");
-  // lambda = A^-T g: the transposed solve, x0 = 0
-  std::vector<double> zero(3 * (size_t)(h->analyzed ? h->an.nb : 0), 0.0);
-  memcpy(lambda, zero.data(), zero.size() * sizeof(double));
-  int rc = solve_impl(h, g_in, lambda, false, true, tol, maxit, res);
+  int rc = check_solve_ready(h);
   if (rc) return rc;
-  if (dA) {
-    const int nb = h->an.nb, n = 3 * nb, g = grid_for(h, n);
-    CK(h->dA.n == (size_t)h->an.nnzb * 9 ? cudaSuccess : (h->dA.release(), h->dA.alloc((size_t)h->an.nnzb * 9)));
-    // lambda and x in the permuted numbering (that of the pattern arrays)
-    CK(cudaMemcpyAsync(h->io64.p, lambda, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, h->io64.p, h->v64.r.p, 1.0);
-    CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, h->io64b.p, h->v64.s.p, 1.0);
-    k_grad_a<<<grid_for(h, nb), kThreads, 0, h->st>>>(nb, h->prowptr.p, h->pcol.p, h->psrc.p,
-                                                      h->v64.r.p, h->v64.s.p, h->dA.p);
-    CK(cudaMemcpyAsync(dA, h->dA.p, (size_t)h->an.nnzb * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    CK(last_error(h));
+  if (dA && h->dA.n != (size_t)h->an.nnzb * 9) {
+    CK(cudaSetDevice(h->opt.device));
+    h->dA.release();
+    CK(h->dA.alloc((size_t)h->an.nnzb * 9));
   }
-  return GBILU_OK;
+  // lambda = A^-T g: the transposed solve, x0 = 0, then dL/dA on the device
+  memset(lambda, 0, 3 * (size_t)h->an.nb * sizeof(double));
+  return solve_impl(h, g_in, lambda, false, true, tol, maxit, res, dA ? x : nullptr, dA);
+}
+
+int gbilu_adjoint_device(void *handle, const double *d_g, const double *d_x, double *d_lambda,
+                         double *d_dA, double tol, int maxit, gbilu_result *res) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!d_g || !d_x || !d_lambda)
+    return h->fail(GBILU_BAD_INPUT, "g, x and lambda must not be NULL");
+  int rc = check_solve_ready(h);
+  if (rc) return rc;
+  CK(cudaSetDevice(h->opt.device));
+  CK(cudaMemsetAsync(d_lambda, 0, 3 * (size_t)h->an.nb * sizeof(double), h->st));
+  return solve_impl(h, d_g, d_lambda, true, true, tol, maxit, res, d_dA ? d_x : nullptr, d_dA);
 }
 
 int gbilu_get_stats(void *handle, gbilu_stats *s) {

@@ -30,6 +30,95 @@ int color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
   return ncolors;
 }
 
+int color_parity_greedy(int nb, const int *rowptr, const int *colind, int *color) {
+  if (nb <= 0) return 0;
+  // 1. Grid edges: an off-diagonal block (u, v) lies on a 4-cycle u-a-b-v
+  //    of the block graph (a != v, b != u). A structured grid's faces all
+  //    do; a non-neighbour connection between distant cells (a fault)
+  //    almost never does.
+  std::vector<char> grid(static_cast<size_t>(rowptr[nb]), 0);
+  std::vector<int> mark(nb, -1);
+  for (int u = 0; u < nb; ++u) {
+    for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) mark[colind[k]] = u;
+    for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
+      const int v = colind[k];
+      if (v == u) continue;
+      bool found = false;
+      // b in N(v) \ {u, v}, then a in N(b) \ {b} with a in N(u) \ {u, v}
+      for (int kb = rowptr[v]; kb < rowptr[v + 1] && !found; ++kb) {
+        const int b = colind[kb];
+        if (b == v || b == u) continue;
+        for (int ka = rowptr[b]; ka < rowptr[b + 1]; ++ka) {
+          const int a = colind[ka];
+          if (a != b && a != u && a != v && mark[a] == u) { found = true; break; }
+        }
+      }
+      grid[k] = found;
+    }
+  }
+  // 2. Distance parity from the lowest-numbered row of each connected part
+  //    of the grid-edge graph (breadth-first; distances do not depend on
+  //    the visiting order).
+  std::vector<int> dist(nb, -1), queue(nb);
+  for (int r = 0; r < nb; ++r) {
+    if (dist[r] >= 0) continue;
+    int head = 0, tail = 0;
+    dist[r] = 0;
+    queue[tail++] = r;
+    while (head < tail) {
+      const int u = queue[head++];
+      for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
+        const int v = colind[k];
+        if (grid[k] && dist[v] < 0) {
+          dist[v] = dist[u] + 1;
+          queue[tail++] = v;
+        }
+      }
+    }
+  }
+  // 3. Every block (u, v), u < v, whose ends have the same parity needs one
+  //    end moved off the two parity colors. Blocks in row-major order: an
+  //    end already moved covers it; else move v unless v touches a moved
+  //    row and u does not (moved rows that touch get a fourth color).
+  std::vector<char> moved(nb, 0);
+  auto touches_moved = [&](int x) {
+    for (int k = rowptr[x]; k < rowptr[x + 1]; ++k)
+      if (moved[colind[k]]) return true;
+    return false;
+  };
+  for (int u = 0; u < nb; ++u)
+    for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
+      const int v = colind[k];
+      if (v <= u || ((dist[u] ^ dist[v]) & 1)) continue;
+      if (moved[u] || moved[v]) continue;
+      if (!touches_moved(v)) moved[v] = 1;
+      else if (!touches_moved(u)) moved[u] = 1;
+      else moved[v] = 1;
+    }
+  // 4. First-fit greedy visiting rows by class (parity 0, parity 1, moved),
+  //    each class in natural order.
+  std::vector<int> order;
+  order.reserve(nb);
+  for (int cls = 0; cls < 3; ++cls)
+    for (int i = 0; i < nb; ++i)
+      if ((moved[i] ? 2 : (dist[i] & 1)) == cls) order.push_back(i);
+  std::vector<int> stamp(static_cast<size_t>(nb) + 1, 0);
+  std::fill(color, color + nb, -1);
+  int ncolors = 0;
+  for (int t = 0; t < nb; ++t) {
+    const int i = order[t];
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int j = colind[k];
+      if (j != i && color[j] >= 0) stamp[color[j]] = t + 1;
+    }
+    int c = 0;
+    while (stamp[c] == t + 1) ++c;
+    color[i] = c;
+    ncolors = std::max(ncolors, c + 1);
+  }
+  return ncolors;
+}
+
 std::string check_pattern(int nb, const int *rowptr, const int *colind) {
   if (nb <= 0) return "nb must be positive";
   // vector entries are indexed with int (3 per block row, 9 per block in
@@ -122,7 +211,7 @@ Csr transpose_csr(int nb, const Csr &m) {
 }  // namespace
 
 std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
-                    bool with_transposes) {
+                    bool with_transposes, int coloring) {
   std::string err = check_pattern(nb, rowptr, colind);
   if (!err.empty()) return err;
   an = Analysis();
@@ -131,7 +220,8 @@ std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
   an.rowptr.assign(rowptr, rowptr + nb + 1);
   an.colind.assign(colind, colind + an.nnzb);
   an.color.resize(nb);
-  an.ncolors = color_greedy(nb, rowptr, colind, an.color.data());
+  an.ncolors = coloring == 1 ? color_greedy(nb, rowptr, colind, an.color.data())
+                             : color_parity_greedy(nb, rowptr, colind, an.color.data());
   const int C = an.ncolors;
 
   // Color-ordered permutation (counting sort). Inside a color, the rows that

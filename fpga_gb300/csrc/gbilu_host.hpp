@@ -63,13 +63,26 @@ struct Analysis {
 // Greedy first-fit coloring in natural row order; returns the color count.
 int color_greedy(int nb, const int *rowptr, const int *colind, int *color);
 
+// Greedy first-fit coloring in an order that follows the grid's two-color
+// parity (the default): blocks on a 4-cycle of the block graph are grid
+// faces; the parity of the breadth-first distance over them from the
+// lowest-numbered row of each connected part two-colors the grid; of each
+// block whose ends have equal parity (a fault connection), one end is
+// moved; rows are then colored first-fit, parity-0 rows first, then
+// parity-1 rows, then the moved rows, each in natural order. On a
+// structured grid with fault connections this gives two large colors and
+// one small one (the moved rows), where natural order cascades into more
+// and larger small colors. Returns the color count.
+int color_parity_greedy(int nb, const int *rowptr, const int *colind, int *color);
+
 // Validates the pattern (sorted unique columns, diagonal present, indices in
 // range, structurally symmetric); returns an empty string when it is fine.
 std::string check_pattern(int nb, const int *rowptr, const int *colind);
 
 // Builds everything above from an input pattern. Returns "" or an error.
+// coloring: 0 color_parity_greedy (default), 1 color_greedy.
 std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
-                    bool with_transposes);
+                    bool with_transposes, int coloring = 0);
 
 // Block ILU(0) (IKJ) of the permuted matrix. pvals (nnzb*9, permuted order)
 // is overwritten with L (col < row) and U (col >= row); dinv[nb*9] gets the

@@ -4,11 +4,13 @@
 // Who needs this: code that runs where it must not allocate device memory --
 // a solver step inside a host framework that hands out a fixed device arena
 // (Flow's linear-solver backends are called between Newton steps and manage
-// their own buffers), a real-time or callback context where cudaMalloc's
-// implicit synchronisation is not allowed, or a caller that records its work
-// into its own CUDA graph and cannot create a gbilu handle there. The handle
-// API allocates its scratch at gbilu_analyze time; this entry point uses no
-// handle and calls no cudaMalloc, cudaFree or allocating library routine.
+// their own buffers), or a real-time or callback context where cudaMalloc's
+// implicit synchronisation is not allowed. The handle API allocates its
+// scratch at gbilu_analyze time; this entry point uses no handle and calls
+// no cudaMalloc, cudaFree or allocating library routine.
+//
+// y is written while x and w are read, with no aliasing between them
+// assumed by the compiler: y must not alias x or w. (w may alias x.)
 //
 // Its only scratch is the file-scope device array below: one partial sum per
 // CTA plus an arrival counter for the grid-wide reduction. Every GPU that
@@ -22,7 +24,11 @@
 // The device address of the array is looked up once per device, on the
 // first call made with that device current (cudaGetSymbolAddress); make that
 // first call before any stream capture, since the lookup is not a stream
-// operation. Later calls only enqueue work on the given stream.
+// operation. Later calls only enqueue work on the given stream. The address
+// belongs to the context that was current at the lookup, the device's
+// primary context when the caller uses the runtime API: calls made with
+// another context current, or after a cudaDeviceReset (which destroys the
+// primary context), would use a stale address, so neither is supported.
 #include "gbilu.h"
 
 #include <cuda_runtime.h>

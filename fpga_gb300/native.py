@@ -27,7 +27,8 @@ class Options(C.Structure):
                 ("inner_tol", C.c_double), ("inner_maxit", C.c_int),
                 ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
                 ("factor_on_device", C.c_int), ("mixed_scheme", C.c_int),
-                ("ru_delta", C.c_double), ("stage_small_steps", C.c_int)]
+                ("ru_delta", C.c_double), ("stage_small_steps", C.c_int),
+                ("coloring", C.c_int)]
 
 
 class Result(C.Structure):
@@ -104,6 +105,8 @@ def load():
     L.gbilu_apply_ilu.argtypes = [VP, F64P, F64P, C.c_int]
     L.gbilu_adjoint.argtypes = [VP, F64P, F64P, F64P, VP, C.c_double, C.c_int,
                                 C.POINTER(Result)]
+    L.gbilu_adjoint_device.argtypes = [VP, VP, VP, VP, VP, C.c_double, C.c_int,
+                                       C.POINTER(Result)]
     L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
     L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
@@ -131,7 +134,7 @@ class GbIlu:
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
                  timeout_ms=0.0, inner_tol=1e-1, inner_maxit=500, max_outer=30,
                  verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
-                 ru_delta=0.1, stage_small_steps=True):
+                 ru_delta=0.1, stage_small_steps=True, coloring="parity"):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -149,6 +152,7 @@ class GbIlu:
         o.mixed_scheme = mixed_scheme
         o.ru_delta = ru_delta
         o.stage_small_steps = int(stage_small_steps)
+        o.coloring = {"parity": 0, "natural": 1}[coloring]
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:
@@ -265,6 +269,14 @@ class GbIlu:
                                          dA.ctypes.data if want_dA else None, tol, maxit,
                                          C.byref(res)))
         return lam, (dA.reshape(-1, 3, 3) if want_dA else None), res
+
+    def adjoint_device(self, g_ptr, x_ptr, lam_ptr, dA_ptr=None, tol=1e-10, maxit=2000):
+        """As adjoint() on device arrays given by address (dA_ptr may be None)."""
+        res = Result()
+        self._check(self.L.gbilu_adjoint_device(self.h, VP(g_ptr), VP(x_ptr), VP(lam_ptr),
+                                                VP(dA_ptr) if dA_ptr else None, tol, maxit,
+                                                C.byref(res)))
+        return res
 
     def stats(self):
         s = Stats()

@@ -94,6 +94,13 @@ typedef struct {
                          when it starts and orders those steps by their data;
                          0: they read global memory and are separated by grid
                          barriers, like the large steps (same results) */
+  int coloring;       /* 0 (default): first-fit greedy in the grid's parity
+                         order -- rows two-colored by the parity of their
+                         distance over blocks that lie on a 4-cycle (grid
+                         faces), one end of each equal-parity block (a fault
+                         connection) moved to the end of the order -- which
+                         leaves one small color on a grid with faults;
+                         1: first-fit greedy in natural row order */
 } gbilu_options;
 
 typedef struct {
@@ -142,7 +149,8 @@ typedef struct {
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
  * no timeout, inner_tol 1e-1, inner_maxit 500, max_outer 30, single-launch
- * sweeps, host factorization, mixed scheme 0, ru_delta 0.1 */
+ * sweeps, host factorization, mixed scheme 0, ru_delta 0.1, small steps
+ * staged, parity-order coloring */
 int gbilu_default_options(gbilu_options *opt);
 
 int gbilu_create(const gbilu_options *opt, void **handle);
@@ -199,6 +207,13 @@ int gbilu_get_factors(void *handle, double *lu, double *dinv);
  * numbering; x holds x0 on entry and the solution on return. tol and maxit
  * follow the reference: maxit full iterations plus the first half of one
  * more (solver.vhd:557, solver_pkg.vhd:127-128). res may be NULL.
+ * In GBILU_MIXED mode maxit caps the FP32 inner half-iterations of all
+ * refinement steps together at 2*maxit + 1 (scheme 0: each inner solve is
+ * also capped by inner_maxit and the steps by max_outer; scheme 1: the one
+ * FP32 run), and a solve stopped by the cap returns GBILU_MAXIT; res->
+ * half_iters is then the total inner half-iterations minus one, the value
+ * the reference's counter would show had all inner halves been one run
+ * (2*maxit at the cap), and res->inner_half_iters the total itself.
  * When both arrays are page-locked (cudaHostAlloc / cudaHostRegister), x0
  * and x move over the CPU-GPU link in place and b by the copy engine while
  * A x0 is computed; other host memory goes through staging copies. Both
@@ -221,11 +236,19 @@ int gbilu_apply_ilu(void *handle, const double *p, double *z, int transpose);
  * x (host arrays, original numbering), solves A^T lambda = g with the
  * transposed SpMV and U^T/L^T sweeps reusing the forward factors, and
  * forms dL/db = lambda and dL/dA = -lambda_i x_j^T on the pattern
- * (dA[nnzb*9] in the analyzed input block order; may be NULL). No
+ * (dA[nnzb*9] in the analyzed input block order; may be NULL). lambda
+ * stays on the device between the solve and the gradient; res->device_ms
+ * covers the whole backward pass (transposed solve and dL/dA). No
  * counterpart in the reference, which has no gradient path. */
 int gbilu_adjoint(void *handle, const double *g, const double *x,
                   double *lambda, double *dA, double tol, int maxit,
                   gbilu_result *res);
+
+/* As gbilu_adjoint with DEVICE pointers (original numbering): d_g[3*nb],
+ * d_x[3*nb] in, d_lambda[3*nb] out (x0 = 0), d_dA[nnzb*9] out or NULL. */
+int gbilu_adjoint_device(void *handle, const double *d_g, const double *d_x,
+                         double *d_lambda, double *d_dA, double tol, int maxit,
+                         gbilu_result *res);
 
 int gbilu_get_stats(void *handle, gbilu_stats *stats);
 
@@ -306,12 +329,17 @@ int gbilu_status_lines(const gbilu_result *res, unsigned long long *buf, int lin
  * (rowptr[nb+1], colind, vals[nnzb*9], x, y, w[3*nb], one double for the
  * dot), enqueued on `stream` (a cudaStream_t, NULL = default stream). No
  * counterpart in the reference. For callers that cannot allocate device
- * memory or create a handle (a fixed device arena, a callback, their own
- * graph capture): it calls no cudaMalloc/cudaFree; its reduction scratch is
- * a fixed ~32 KiB device array inside the library, which limits nb to
- * 1,048,576 block rows (larger nb -> GBILU_BAD_INPUT). The first call on a
- * device looks that array up and should precede any stream capture; calls
- * that overlap on the GPU share the array and race. */
+ * memory or create a handle (a host framework that hands out a fixed
+ * device arena, a callback in which cudaMalloc's implicit synchronisation
+ * is not allowed): it calls no cudaMalloc/cudaFree; its reduction scratch
+ * is a fixed ~32 KiB device array inside the library, which limits nb to
+ * 1,048,576 block rows (larger nb -> GBILU_BAD_INPUT). y must not alias x
+ * or w (w may alias x). The first call on a device looks the array's
+ * address up in the device's primary context (the CUDA runtime's) and
+ * keeps it for the life of the process: make that first call before any
+ * stream capture, call it with the primary context current, and not
+ * across a cudaDeviceReset. Calls that overlap on the GPU share the array
+ * and race. */
 int gbilu_bsr_spmv_dot_noalloc(int nb, const int *d_rowptr, const int *d_colind,
                                const double *d_vals, const double *d_x, double *d_y,
                                const double *d_w, double *d_dot, void *stream);

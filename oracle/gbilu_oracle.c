@@ -40,6 +40,97 @@ int orc_color_greedy(int nb, const int *rowptr, const int *colind, int *color) {
   return ncolors;
 }
 
+/* 1 when the sorted column lists of rows a and v share a row other than
+ * the excluded ones (x1, x2, a and v themselves) */
+static int shares_other(const int *rowptr, const int *colind, int a, int v, int x1, int x2) {
+  int p = rowptr[a], q = rowptr[v];
+  while (p < rowptr[a + 1] && q < rowptr[v + 1]) {
+    int ca = colind[p], cv = colind[q];
+    if (ca < cv) { ++p; continue; }
+    if (cv < ca) { ++q; continue; }
+    if (ca != x1 && ca != x2 && ca != a && ca != v) return 1;
+    ++p; ++q;
+  }
+  return 0;
+}
+
+int orc_color_parity(int nb, const int *rowptr, const int *colind, int *color) {
+  size_t nnzb = (size_t)rowptr[nb];
+  /* (1) face[k]: block k = (u, v) lies on a 4-cycle u - a - b - v - u with
+   * a, b outside {u, v}: some a in N(u) shares a neighbour b != u with v */
+  char *face = (char *)calloc(nnzb + 1, 1);
+  for (int u = 0; u < nb; ++u)
+    for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
+      int v = colind[k];
+      if (v == u) continue;
+      for (int ka = rowptr[u]; ka < rowptr[u + 1] && !face[k]; ++ka) {
+        int a = colind[ka];
+        if (a == u || a == v) continue;
+        if (shares_other(rowptr, colind, a, v, u, v)) face[k] = 1;
+      }
+    }
+  /* (2) distance parity over face blocks from the lowest-numbered row of
+   * each connected part, level by level */
+  int *dist = (int *)malloc(sizeof(int) * (size_t)(nb > 0 ? nb : 1));
+  int *cur = (int *)malloc(sizeof(int) * (size_t)(nb > 0 ? nb : 1));
+  int *nxt = (int *)malloc(sizeof(int) * (size_t)(nb > 0 ? nb : 1));
+  for (int i = 0; i < nb; ++i) dist[i] = -1;
+  for (int root = 0; root < nb; ++root) {
+    if (dist[root] >= 0) continue;
+    int ncur = 1, level = 0;
+    cur[0] = root;
+    dist[root] = 0;
+    while (ncur > 0) {
+      int nn = 0;
+      ++level;
+      for (int t = 0; t < ncur; ++t) {
+        int u = cur[t];
+        for (int k = rowptr[u]; k < rowptr[u + 1]; ++k)
+          if (face[k] && dist[colind[k]] < 0) {
+            dist[colind[k]] = level;
+            nxt[nn++] = colind[k];
+          }
+      }
+      int *tmp = cur; cur = nxt; nxt = tmp;
+      ncur = nn;
+    }
+  }
+  /* (3) blocks (u, v), u < v, of equal parity, in row-major order: unless
+   * an end is already moved, move v -- or u when v has a moved neighbour
+   * and u has none */
+  char *moved = (char *)calloc((size_t)nb + 1, 1);
+  for (int u = 0; u < nb; ++u)
+    for (int k = rowptr[u]; k < rowptr[u + 1]; ++k) {
+      int v = colind[k];
+      if (v <= u || (dist[u] & 1) != (dist[v] & 1) || moved[u] || moved[v]) continue;
+      int vm = 0, um = 0;
+      for (int q = rowptr[v]; q < rowptr[v + 1]; ++q) vm |= moved[colind[q]];
+      for (int q = rowptr[u]; q < rowptr[u + 1]; ++q) um |= moved[colind[q]];
+      if (vm && !um) moved[u] = 1; else moved[v] = 1;
+    }
+  /* (4) first-fit greedy over rows ordered (parity 0, parity 1, moved),
+   * natural order inside each class */
+  int *mark = (int *)calloc((size_t)nb + 2, sizeof(int));
+  int ncolors = 0, step = 0;
+  for (int i = 0; i < nb; ++i) color[i] = -1;
+  for (int cls = 0; cls < 3; ++cls)
+    for (int i = 0; i < nb; ++i) {
+      int ci = moved[i] ? 2 : (dist[i] & 1);
+      if (ci != cls) continue;
+      ++step;
+      for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+        int j = colind[k];
+        if (j != i && color[j] >= 0) mark[color[j]] = step;
+      }
+      int c = 0;
+      while (mark[c] == step) ++c;
+      color[i] = c;
+      if (c + 1 > ncolors) ncolors = c + 1;
+    }
+  free(face); free(dist); free(cur); free(nxt); free(moved); free(mark);
+  return ncolors;
+}
+
 void orc_color_order(int nb, const int *rowptr, const int *colind,
                      const int *color, int ncolors, int *perm, int *color_ptr,
                      int *split) {

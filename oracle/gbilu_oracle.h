@@ -42,6 +42,18 @@ enum {
  * neighbour. Returns the number of colors. */
 int orc_color_greedy(int nb, const int *rowptr, const int *colind, int *color);
 
+/* Greedy first-fit coloring in the grid's parity order (the default of the
+ * product): (1) a block (u, v) is a face when it lies on a 4-cycle
+ * u - a - b - v - u of the block graph with a, b outside {u, v}; (2) every
+ * row gets the parity of its breadth-first distance over face blocks from
+ * the lowest-numbered row of its connected part; (3) the off-diagonal
+ * blocks (u, v), u < v, whose ends have equal parity are visited in
+ * row-major order: if neither end is moved yet, v is moved -- except that
+ * u is moved when v has a moved neighbour and u has none; (4) rows are
+ * colored first-fit in the order: parity-0 rows, parity-1 rows, moved rows,
+ * natural order inside each class. Returns the number of colors. */
+int orc_color_parity(int nb, const int *rowptr, const int *colind, int *color);
+
 /* perm[new] = old: rows ordered by color; inside a color, the rows that
  * share a block with a row of a higher color (as either end) come first,
  * then the others, each group in natural order. color_ptr[c]..color_ptr[c+1]

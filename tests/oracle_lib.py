@@ -37,6 +37,8 @@ def lib():
         L = C.CDLL(ORACLE_SO)
         L.orc_color_greedy.argtypes = [C.c_int, I32P, I32P, I32P]
         L.orc_color_greedy.restype = C.c_int
+        L.orc_color_parity.argtypes = [C.c_int, I32P, I32P, I32P]
+        L.orc_color_parity.restype = C.c_int
         L.orc_color_order.argtypes = [C.c_int, I32P, I32P, I32P, C.c_int, I32P, I32P,
                                       I32P]
         L.orc_permute_bsr.argtypes = [C.c_int, I32P, I32P, F64P, I32P, I32P,
@@ -71,7 +73,7 @@ def lib():
 class Prepared:
     """Colored, permuted and factored copy of a BlockSystem (oracle side)."""
 
-    def __init__(self, sysm):
+    def __init__(self, sysm, coloring="parity"):
         L = lib()
         self.sys = sysm
         nb = sysm.nb
@@ -79,7 +81,8 @@ class Prepared:
         rp = np.ascontiguousarray(sysm.rowptr, dtype=np.int32)
         ci = np.ascontiguousarray(sysm.colind, dtype=np.int32)
         self.color = np.empty(nb, np.int32)
-        self.ncolors = L.orc_color_greedy(nb, rp, ci, self.color)
+        color_fn = {"parity": L.orc_color_parity, "natural": L.orc_color_greedy}[coloring]
+        self.ncolors = color_fn(nb, rp, ci, self.color)
         self.perm = np.empty(nb, np.int32)
         self.color_ptr = np.empty(self.ncolors + 1, np.int32)
         self.split = np.empty(self.ncolors, np.int32)

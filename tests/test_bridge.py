@@ -80,3 +80,21 @@ def test_bridge_solves_match_oracle(driver, tmp_path, precision):
         scale = 1.0 if x is x1 else 1.5
         rel = np.linalg.norm(s.b - scale * (A @ x)) / np.linalg.norm(s.b)
         assert rel <= tol * (1 + 1e-6) and abs(rel - r["reduction"]) <= 1e-3 * tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("maxit", [0, 2, 5])
+def test_bridge_mixed_honours_maxit(driver, tmp_path, maxit):
+    """A simulator backend's iteration limit bounds a mixed-precision solve:
+    the FP32 inner half-iterations of all refinement steps stop at
+    2*maxit + 1, and the result reports MAXIT (not converged)."""
+    s = make_config("c1_20x20x10")
+    head, res, x1, _ = run_driver(driver, tmp_path, s, device=0, precision=1, tol=1e-13,
+                                  maxit=maxit)
+    assert tuple(int(v) for v in head[:3]) == (0, 0, 0)
+    for r in res:
+        assert r["status"] == 1 and not r["converged"]
+        assert r["half_iters"] == 2 * maxit
+    A = s.to_scipy()
+    rel = np.linalg.norm(s.b - A @ x1) / np.linalg.norm(s.b)
+    assert abs(rel - res[0]["reduction"]) <= 1e-6 * rel

@@ -18,7 +18,10 @@ from fpga_gb300 import load, native
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF_SO = os.path.join(ROOT, "oracle", "_ref", "libfpgaref.so")
-REFERENCE = "/root/reference/linearalgebra/ilu0bicgstab/xilinx/src/sda_app"
+# the reference tree (read only to build the checker); GBILU_REFERENCE_ROOT
+# overrides where it is
+REFERENCE_ROOT = os.environ.get("GBILU_REFERENCE_ROOT", "/root/reference")
+REFERENCE = os.path.join(REFERENCE_ROOT, "linearalgebra/ilu0bicgstab/xilinx/src/sda_app")
 
 I32P = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 U64P = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
@@ -29,7 +32,8 @@ I64P = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
 @pytest.fixture(scope="module")
 def ref():
     if os.path.isdir(REFERENCE):
-        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")])
+        subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"),
+                               f"REF={REFERENCE}"])
     elif not os.path.exists(REF_SO):
         pytest.skip("reference host library not built and reference tree absent")
     L = C.CDLL(REF_SO)

@@ -255,6 +255,30 @@ def test_maxit_semantics(case, maxit):
     assert rel(x, x_ref) < 1e-10
 
 
+@pytest.mark.parametrize("scheme", [0, 1])
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_mixed_maxit_semantics(built_lib, scheme, use_graph):
+    """maxit caps the mixed solve's inner half-iterations of all refinement
+    steps together at 2*maxit + 1, as the reference caps one run; the
+    counter then reads 2*maxit and the status is MAXIT."""
+    s = CASES["faults"]()
+    with GbIlu(device=0, precision="mixed", mixed_scheme=scheme, use_graph=use_graph) as m:
+        m.analyze(s.rowptr, s.colind).factor(s.vals)
+        for maxit in (0, 1, 2, 3, 7):
+            x, r = m.solve(s.b, tol=1e-14, maxit=maxit)
+            assert r.status == 1, (maxit, r.status)
+            assert r.half_iters == 2 * maxit, (maxit, r.half_iters)
+            assert r.inner_half_iters == 2 * maxit + 1, (maxit, r.inner_half_iters)
+            true = np.linalg.norm(s.b - s.to_scipy() @ x) / np.linalg.norm(s.b)
+            assert abs(r.true_relres - true) <= 1e-6 * true
+        # inner_maxit still caps each refinement step, maxit the total
+        if scheme == 0:
+            with GbIlu(device=0, precision="mixed", inner_maxit=1, max_outer=50) as m2:
+                m2.analyze(s.rowptr, s.colind).factor(s.vals)
+                x, r = m2.solve(s.b, tol=1e-14, maxit=4)
+                assert r.status == 1 and r.inner_half_iters == 9 and r.outer_iters >= 3
+
+
 def test_warm_start(case):
     s, P, g = case
     x0 = np.random.default_rng(3).standard_normal(s.n) * 0.1

@@ -27,11 +27,12 @@ def test_exports_every_declared_symbol(built_lib):
         assert hasattr(lib, name), name
 
 
+@pytest.mark.parametrize("coloring", ["parity", "natural"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_host_analysis_matches_oracle(built_lib, name):
+def test_host_analysis_matches_oracle(built_lib, name, coloring):
     s = CASES[name]()
-    P = Prepared(s)
-    with GbIlu(device=-1) as g:
+    P = Prepared(s, coloring=coloring)
+    with GbIlu(device=-1, coloring=coloring) as g:
         g.analyze(s.rowptr, s.colind).factor(s.vals)
         nc, color, perm, cp = g.ordering()
         assert nc == P.ncolors
@@ -97,3 +98,47 @@ def test_error_behaviour(built_lib):
 def test_status_strings(built_lib):
     for code in range(11):
         assert native.status_string(code) != "unknown status"
+
+
+def random_symmetric(nb, density, seed):
+    """A random structurally symmetric pattern with the diagonal."""
+    rng = np.random.default_rng(seed)
+    m = rng.random((nb, nb)) < density
+    m = m | m.T | np.eye(nb, dtype=bool)
+    rowptr = np.concatenate([[0], np.cumsum(m.sum(1))]).astype(np.int32)
+    colind = np.concatenate([np.flatnonzero(r) for r in m]).astype(np.int32)
+    return nb, rowptr, colind
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_parity_coloring_general_patterns(built_lib, seed):
+    """The parity-order coloring on patterns that are not grids (random
+    symmetric, from sparse to dense): a valid coloring, identical to the
+    oracle's separate implementation."""
+    nb, rowptr, colind = random_symmetric(40 + 30 * seed, [0.01, 0.03, 0.1, 0.3, 0.02, 0.05][seed],
+                                          seed)
+    L = __import__("oracle_lib").lib()
+    ref = np.empty(nb, np.int32)
+    nref = L.orc_color_parity(nb, rowptr, colind, ref)
+    with GbIlu(device=-1) as g:
+        g.analyze(rowptr, colind)
+        nc, color, perm, cp = g.ordering()
+    assert nc == nref and np.array_equal(color, ref)
+    rows = np.repeat(np.arange(nb), np.diff(rowptr))
+    off = rows != colind
+    assert not np.any(color[rows[off]] == color[colind[off]])
+
+
+def test_parity_coloring_grid_with_faults(built_lib):
+    """On the 500k-cell system with fault connections the parity order
+    leaves two large colors and one small one; natural order gives five."""
+    s = make_config("c2_100x100x50")
+    with GbIlu(device=-1) as g:
+        g.analyze(s.rowptr, s.colind)
+        nc, _, _, cp = g.ordering()
+    with GbIlu(device=-1, coloring="natural") as g:
+        g.analyze(s.rowptr, s.colind)
+        nc_nat = g.ordering()[0]
+    sizes = np.diff(cp)
+    assert nc == 3 and nc_nat == 5
+    assert sizes[2] < 0.01 * s.nb

@@ -187,7 +187,8 @@ def golden_system(f):
                        np.arange(nb), tuple(int(v) for v in f["grid"]))
 
 
-@pytest.mark.parametrize("name", ["golden_small.npz", "golden_faults.npz"])
+@pytest.mark.parametrize("name", ["golden_small.npz", "golden_faults.npz",
+                                  "golden_faults_natural.npz"])
 def test_golden_fixtures(name):
     f = np.load(os.path.join(GOLDEN, name))
     # the generator reproduces the stored system (structure exactly; values to
@@ -198,7 +199,7 @@ def test_golden_fixtures(name):
     assert np.array_equal(g.rowptr, f["rowptr"]) and np.array_equal(g.colind, f["colind"])
     assert np.allclose(g.vals.reshape(-1), f["vals"], rtol=1e-14, atol=0)
     s = golden_system(f)
-    P = Prepared(s)
+    P = Prepared(s, coloring=str(f["coloring"]))
     assert P.ncolors == int(f["ncolors"])
     assert np.array_equal(P.color, f["color"]) and np.array_equal(P.perm, f["perm"])
     assert np.array_equal(P.split, f["split"])
