@@ -118,6 +118,8 @@ struct Handle {
   int stage_bytes[2][2] = {};
   DevBuf<StageEntry> stage_tab[2][2];
   DevBuf<int2> stage_cnt[2][2];
+  DevBuf<unsigned int> ring_tab[2][2];     // streamed slices per CTA (see StagePlan)
+  DevBuf<int> ring_cnt[2][2];
   cudaError_t launch_err = cudaSuccess;    // first failed cooperative launch
   int coop_grid64 = 1, coop_grid32 = 1;    // CTAs of the cooperative apply
   size_t device_bytes = 0;
@@ -270,30 +272,42 @@ int coop_grid(Handle *h) {
 // dealt round-robin to the CTAs of the cooperative grid; each CTA's entries
 // pack [values | column indices | D^-1] at 128-byte multiples. Staging is
 // off for this (precision, direction) when a CTA would need more than
-// kStageBudget bytes or kMaxStage entries.
+// kStageBudget bytes or kMaxStage entries. The large steps' ring takes the
+// shared memory left after the staged slices.
 constexpr int kStageBudget = 160 * 1024;
+constexpr int kRingMin = 4;   // fewer ring stages than this: no ring
+
+// Bytes of one slice's [values | column indices | D block] in shared memory.
+template <typename V>
+long long slice_bytes(const SlicedMatrix &m, int slice, bool uses_d) {
+  const long long w = m.off[slice + 1] - m.off[slice];
+  return w * 9 * 32 * (long long)sizeof(V) + w * 32 * (long long)sizeof(int) +
+         (uses_d ? 9 * 32 * (long long)sizeof(V) : 0);
+}
 
 template <typename V, typename T>
 int build_stage_plan(Handle *h, int f, int t, int grid) {
   PhaseList &pl = h->phases[f][t];
   const Analysis &an = h->an;
+  auto mat_of = [&](const Phase &P) -> const SlicedMatrix & {
+    return t == 0 ? (P.mat ? an.U : an.L) : (P.mat ? an.Lt : an.Ut);
+  };
   std::vector<std::vector<StageEntry>> per(grid);
   std::vector<long long> bytes(grid, 0);
   for (int q = 0; q < pl.n; ++q) {
     Phase &P = pl.p[q];
     P.staged = 0;
+    P.streamed = 0;
     if (P.nrows > kSmallRows) continue;
-    const SlicedMatrix &m = t == 0 ? (P.mat ? an.U : an.L) : (P.mat ? an.Lt : an.Ut);
+    const SlicedMatrix &m = mat_of(P);
     const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
     // steps linked by a CTA barrier (local_after) all run on CTA 0
     const bool local = P.local_after || (q > 0 && pl.p[q - 1].local_after);
     for (int j = 0; j < nsl; ++j) {
       const int b = local ? 0 : (j + q) % grid;
-      const int w = m.off[P.slice0 + j + 1] - m.off[P.slice0 + j];
-      const long long sz = (long long)w * 9 * 32 * sizeof(V) + (long long)w * 32 * sizeof(int) +
-                           (P.uses_d() ? 9 * 32 * (long long)sizeof(V) : 0);
-      per[b].push_back(StageEntry{q, j, w, (int)bytes[b]});
-      bytes[b] += sz;
+      per[b].push_back(StageEntry{q, j, m.off[P.slice0 + j + 1] - m.off[P.slice0 + j],
+                                  (int)bytes[b]});
+      bytes[b] += slice_bytes<V>(m, P.slice0 + j, P.uses_d());
     }
     P.staged = 1;
   }
@@ -303,32 +317,98 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
     most = std::max(most, bytes[b]);
     most_n = std::max(most_n, per[b].size());
   }
-  h->stage[f][t] = StagePlan{nullptr, nullptr, 0};
+  h->stage[f][t] = StagePlan{nullptr, nullptr, 0, 0, 0, 0, nullptr, nullptr, 0};
   h->stage_bytes[f][t] = 0;
-  if (!h->opt.stage_small_steps || most_n == 0 || most > kStageBudget ||
-      most_n > (size_t)kMaxStage) {
+  const bool staged = h->opt.stage_small_steps && most_n > 0 && most <= kStageBudget &&
+                      most_n <= (size_t)kMaxStage;
+  if (!staged) {
     for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
-    return GBILU_OK;
+    most = 0;
   }
-  std::vector<StageEntry> tab((size_t)grid * kMaxStage, StageEntry{0, 0, 0, 0});
-  std::vector<int2> cnt(grid);
-  for (int b = 0; b < grid; ++b) {
-    for (size_t e = 0; e < per[b].size(); ++e) tab[(size_t)b * kMaxStage + e] = per[b][e];
-    cnt[b] = make_int2((int)per[b].size(), (int)bytes[b]);
+  // the ring of the large (not staged) steps, after the staged slices
+  int optin = 0;
+  CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->opt.device));
+  cudaFuncAttributes fa;
+  CK(cudaFuncGetAttributes(&fa, k_ilu_coop<V, T>));
+  const long long ring_off = (most + 127) / 128 * 128;
+  long long stride = 0;
+  bool any_large = false;
+  for (int q = 0; q < pl.n; ++q) {
+    const Phase &P = pl.p[q];
+    if (P.staged || P.nrows <= kSmallRows) continue;
+    any_large = true;
+    const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
+    for (int j = 0; j < nsl; ++j)
+      stride = std::max(stride, slice_bytes<V>(mat_of(P), P.slice0 + j, P.uses_d()));
   }
-  CK(h->stage_tab[f][t].alloc(tab.size()));
-  CK(h->stage_cnt[f][t].alloc(cnt.size()));
-  CK(cudaMemcpy(h->stage_tab[f][t].p, tab.data(), tab.size() * sizeof(StageEntry), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(h->stage_cnt[f][t].p, cnt.data(), cnt.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  CK(cudaFuncSetAttribute(k_ilu_coop<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, kStageBudget));
-  int per_sm = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, coop_threads<T>(), (size_t)most));
-  if (per_sm < 1) {
-    for (int q = 0; q < pl.n; ++q) pl.p[q].staged = 0;
-    return GBILU_OK;
+  stride = (stride + 127) / 128 * 128;
+  const long long avail = (long long)optin - (long long)fa.sharedSizeBytes - ring_off;
+  const int ns = (stride > 0 && avail > 0) ? (int)std::min<long long>(kRingMax, avail / stride) : 0;
+  const bool ring = h->opt.stream_large_steps && any_large && ns >= kRingMin;
+  if (ring)
+    for (int q = 0; q < pl.n; ++q)
+      pl.p[q].streamed = !pl.p[q].staged && pl.p[q].nrows > kSmallRows;
+  const long long dyn = ring ? ring_off + ns * stride : most;
+  if (dyn > 0) {
+    CK(cudaFuncSetAttribute(k_ilu_coop<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)std::max<long long>(dyn, fa.maxDynamicSharedSizeBytes)));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ilu_coop<V, T>, coop_threads<T>(),
+                                                     (size_t)dyn));
+    if (per_sm < 1)
+      return h->fail(GBILU_CUDA_ERROR, "single-launch apply does not fit an SM with %lld bytes "
+                     "of shared memory", dyn);
   }
-  h->stage[f][t] = StagePlan{h->stage_tab[f][t].p, h->stage_cnt[f][t].p, 1};
-  h->stage_bytes[f][t] = (int)most;
+  StagePlan sp{nullptr, nullptr, 0, ring ? ns : 0, ring ? (int)stride : 0, (int)ring_off,
+               nullptr, nullptr, 0};
+  if (ring) {
+    // each CTA's streamed slices in launch order: slice j of a step goes to
+    // CTA j % grid
+    std::vector<std::vector<unsigned int>> lists(grid);
+    for (int q = 0; q < pl.n; ++q) {
+      const Phase &P = pl.p[q];
+      if (!P.streamed) continue;
+      const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
+      for (int j = 0; j < nsl; ++j)
+        lists[j % grid].push_back((unsigned int)(P.slice0 + j) | ((unsigned int)P.mat << 30) |
+                                  ((unsigned int)P.uses_d() << 31));
+    }
+    size_t mx = 1;
+    for (const auto &l : lists) mx = std::max(mx, l.size());
+    std::vector<unsigned int> tab(mx * grid, 0u);
+    std::vector<int> cnt(grid);
+    for (int b = 0; b < grid; ++b) {
+      std::copy(lists[b].begin(), lists[b].end(), tab.begin() + (size_t)b * mx);
+      cnt[b] = (int)lists[b].size();
+    }
+    CK(h->ring_tab[f][t].alloc(tab.size()));
+    CK(h->ring_cnt[f][t].alloc(cnt.size()));
+    CK(cudaMemcpy(h->ring_tab[f][t].p, tab.data(), tab.size() * sizeof(unsigned int),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->ring_cnt[f][t].p, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
+    sp.ring_tab = h->ring_tab[f][t].p;
+    sp.ring_cnt = h->ring_cnt[f][t].p;
+    sp.ring_max = (int)mx;
+  }
+  if (staged) {
+    std::vector<StageEntry> tab((size_t)grid * kMaxStage, StageEntry{0, 0, 0, 0});
+    std::vector<int2> cnt(grid);
+    for (int b = 0; b < grid; ++b) {
+      for (size_t e = 0; e < per[b].size(); ++e) tab[(size_t)b * kMaxStage + e] = per[b][e];
+      cnt[b] = make_int2((int)per[b].size(), (int)bytes[b]);
+    }
+    CK(h->stage_tab[f][t].alloc(tab.size()));
+    CK(h->stage_cnt[f][t].alloc(cnt.size()));
+    CK(cudaMemcpy(h->stage_tab[f][t].p, tab.data(), tab.size() * sizeof(StageEntry),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->stage_cnt[f][t].p, cnt.data(), cnt.size() * sizeof(int2),
+                  cudaMemcpyHostToDevice));
+    sp.tab = h->stage_tab[f][t].p;
+    sp.cnt = h->stage_cnt[f][t].p;
+    sp.enabled = 1;
+  }
+  h->stage[f][t] = sp;
+  h->stage_bytes[f][t] = (int)dyn;
   return GBILU_OK;
 }
 
@@ -579,7 +659,9 @@ void release_device(Handle *h) {
     for (int t = 0; t < 2; ++t) {
       h->stage_tab[f][t].release();
       h->stage_cnt[f][t].release();
-      h->stage[f][t] = StagePlan{nullptr, nullptr, 0};
+      h->ring_tab[f][t].release();
+      h->ring_cnt[f][t].release();
+      h->stage[f][t] = StagePlan{nullptr, nullptr, 0, 0, 0, 0, nullptr, nullptr, 0};
       h->stage_bytes[f][t] = 0;
     }
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
@@ -945,6 +1027,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->ru_delta = 0.1;
   o->stage_small_steps = 1;
   o->coloring = 0;
+  o->stream_large_steps = 0;
   return GBILU_OK;
 }
 
@@ -1319,6 +1402,11 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   s->last_launches = h->last_launches;
   s->factor_ms = h->factor_ms;
   s->analyze_ms = h->analyze_ms;
+  for (int p = 0; p < 2; ++p) {
+    s->ring_stages[p] = h->stage[p][0].ring_ns;
+    s->ring_stage_bytes[p] = h->stage[p][0].ring_stride;
+    s->apply_smem_bytes[p] = h->stage_bytes[p][0];
+  }
   for (int p = 0; p < 2; ++p) {
     const double sv = p ? 4.0 : 8.0, sx = sv, si = 4.0;
     const double nb = an.nb, n = 3.0 * an.nb;

@@ -432,6 +432,8 @@ struct Phase {
                     // CTA 0: a CTA barrier between them instead of a grid one
   int flow_after;   // this step and the next are small: when both are staged,
                     // no barrier -- the next step waits for the values it reads
+  int streamed;     // a large step whose slices a producer warp streams into
+                    // a shared-memory ring ahead of the compute warps
   // whether a D block of the step's rows is read
   __host__ __device__ bool uses_d() const { return has_d || (to_y && final_d); }
 };
@@ -520,10 +522,27 @@ struct StageEntry {
 };
 constexpr int kMaxStage = 64;         // entries per CTA
 
+// Large color steps stream their slices through a ring of ring_ns stages
+// of ring_stride bytes at byte offset ring_off of the dynamic shared memory
+// (after the staged small steps): the producer warp copies a slice's
+// [values | column indices | D block] with bulk copies as soon as its stage
+// is free -- running ahead into the next large step while the small steps
+// and barriers in between run -- and the compute warps take the slices in
+// turn. ring_ns = 0: no ring, every warp computes and the large steps load
+// their matrix rows directly.
+constexpr int kRingMax = 16;
+
 struct StagePlan {
   const StageEntry *tab;              // [grid][kMaxStage]
   const int2 *cnt;                    // per CTA: entries, total bytes
   int enabled;
+  int ring_ns, ring_stride, ring_off;
+  // per CTA, its streamed slices in launch order: entry g of CTA b at
+  // ring_tab[b * ring_max + g] = slice | matrix << 30 | uses_d << 31
+  // (matrix 1: the second sweep's), ring_cnt[b] of them
+  const unsigned int *ring_tab;
+  const int *ring_cnt;
+  int ring_max;
 };
 
 constexpr unsigned int kStageSpins = 1u << 22;
@@ -548,6 +567,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
   return ok != 0;
+}
+// non-blocking phase test (try_wait may suspend the thread for a while,
+// which in a divergent warp holds up the other lanes)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 // global -> shared bulk copy (16-byte aligned ends, size a multiple of 16),
 // completion counted on the mbarrier
@@ -607,9 +641,27 @@ __device__ __forceinline__ void mark_stage_timeout(Ctl *c) {
   atomicExch(&c->done, 1);
 }
 
-__device__ __forceinline__ bool grid_barrier(Ctl *c, bool late = false) {
+// CTA barriers over the first nthreads threads (named barrier 7): the
+// compute warps of the single-launch apply, which leaves its producer warp
+// out of them once the two roles split.
+__device__ __forceinline__ void cta_sync(int nthreads) {
+  asm volatile("bar.sync 7, %0;" ::"r"(nthreads) : "memory");
+}
+__device__ __forceinline__ int cta_sync_or(int nthreads, int pred) {
+  int r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.or.pred q, 7, %2, p;\n"
+      " selp.s32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"(pred), "r"(nthreads)
+      : "memory");
+  return r;
+}
+
+__device__ __forceinline__ bool grid_barrier(Ctl *c, bool late = false, int nthreads = 0) {
   __shared__ int ok;
-  const int any_late = __syncthreads_or(late);
+  if (nthreads == 0) nthreads = blockDim.x;
+  const int any_late = cta_sync_or(nthreads, late);
   if (threadIdx.x == 0) {
     ok = !any_late;
     if (any_late) mark_stage_timeout(c);
@@ -629,7 +681,7 @@ __device__ __forceinline__ bool grid_barrier(Ctl *c, bool late = false) {
       if (spins > 256) __nanosleep(32);
     }
   }
-  __syncthreads();
+  cta_sync(nthreads);
   return ok != 0;
 }
 
@@ -691,7 +743,9 @@ template <typename V, typename T>
 __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, int w, const V *sv,
                                            const int *sc, const V *sd, const T *src, T *ybuf,
                                            T *hat, Ctl *ctl) {
-  constexpr int SB = sizeof(T) == 8 ? 4 : 8;   // gathers in flight per batch
+  // gathers in flight per batch (8 in FP32 spilled once the ring's state
+  // was added to the kernel)
+  constexpr int SB = sizeof(T) == 8 ? 4 : 6;
   const T *own = P.own_y ? ybuf : src;
   const T *nbr = P.nbr_hat ? hat : ybuf;
   // only values of ybuf and hat can be sentinels: reads of the input src are
@@ -806,13 +860,149 @@ __device__ __forceinline__ void group_sync(int g) {
   asm volatile("bar.sync %0, 96;" ::"r"(1 + g) : "memory");
 }
 
+// Bounded mbarrier phase wait of the ring. Gives up after kStageSpins
+// polls, or early once another wait of the run failed. A parity wait only
+// tells the current phase of a barrier from the one before it, so a waiter
+// must never be two phases ahead: the producer waits for the phases of a
+// stage's free barrier one after another, and a compute warp first waits
+// until the stage's sequence word names its slice (the producer writes it
+// only once the previous round of that stage was consumed, hence filled),
+// then for the fill itself.
+__device__ __forceinline__ bool ring_wait(Ctl *ctl, uint64_t *bar, uint32_t parity) {
+  unsigned int spins = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++spins > kStageSpins || ((spins & 1023) == 0 && *(volatile int *)&ctl->bar_fail))
+      return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool ring_wait_slice(Ctl *ctl, const unsigned int *seq, unsigned int g,
+                                                uint64_t *bar, uint32_t parity) {
+  unsigned int spins = 0;
+  while (*(volatile const unsigned int *)seq != g) {
+    if (++spins > kStageSpins || ((spins & 1023) == 0 && *(volatile int *)&ctl->bar_fail))
+      return false;
+    if (spins > 64) __nanosleep(32);
+  }
+  return ring_wait(ctl, bar, parity);
+}
+
+// Producer of the ring, one lane per stage: the CTA's slices of the
+// streamed steps, numbered in launch order (the host lists them), and lane
+// st of the producer warp fills stage st with the slices g = st (mod ns),
+// each once the compute warp that held the slice g - ns released the
+// stage. The warp stays converged: every pass each lane tests (without
+// blocking) whether its stage is free and, if so, issues the fill and loads
+// the slot range of its next slice. Before it returns every lane waits for
+// its own last copies, so that the CTA never ends with a bulk copy in
+// flight.
+template <typename V>
+__device__ void ring_produce(Ctl *ctl, const StagePlan &sp, unsigned char *ring, uint64_t *full,
+                             uint64_t *empty, int *ring_w, unsigned int *ring_seq,
+                             const int *off1, const int *col1, const V *val1, const int *off2,
+                             const int *col2, const V *val2, const V *dmat, unsigned int st) {
+  const unsigned int ns = (unsigned int)sp.ring_ns;
+  const unsigned int total = (unsigned int)sp.ring_cnt[blockIdx.x];
+  const unsigned int *tab = sp.ring_tab + (size_t)blockIdx.x * sp.ring_max;
+  unsigned int g = st, k = 0;   // next slice of this lane, fills so far
+  bool active = st < ns && g < total;
+  unsigned int ent = 0;
+  int o = 0, w = 0;
+  auto load = [&]() {
+    ent = __ldg(tab + g);
+    const int *off = (ent >> 30) & 1u ? off2 : off1;
+    const int sl = (int)(ent & 0x3fffffffu);
+    o = __ldg(off + sl);
+    w = __ldg(off + sl + 1) - o;
+  };
+  if (active) load();
+  unsigned int spins = 0;
+  bool ok = true;
+  while (__any_sync(0xffffffffu, active)) {
+    if (active) {
+      if (k == 0 || mbar_test_wait(&empty[st], (k - 1) & 1u)) {
+        const int sl = (int)(ent & 0x3fffffffu);
+        const bool m2 = (ent >> 30) & 1u;
+        const int *col = m2 ? col2 : col1;
+        const V *val = m2 ? val2 : val1;
+        const uint32_t vb = (uint32_t)(w * 9 * 32 * sizeof(V)), cb = (uint32_t)(w * 32 * sizeof(int));
+        const uint32_t db = (ent >> 31) ? (uint32_t)(9 * 32 * sizeof(V)) : 0u;
+        unsigned char *dst = ring + (size_t)st * sp.ring_stride;
+        ring_w[st] = w;
+        // the slice number: a compute warp waits for it before the fill
+        *(volatile unsigned int *)&ring_seq[st] = g;
+        mbar_expect_tx(&full[st], vb + cb + db);   // this lane's arrival, released to the waiters
+        if (vb) bulk_g2s(dst, val + (size_t)o * 9 * 32, vb, &full[st]);
+        if (cb) bulk_g2s(dst + vb, col + (size_t)o * 32, cb, &full[st]);
+        if (db) bulk_g2s(dst + vb + cb, dmat + (size_t)sl * 9 * 32, db, &full[st]);
+        g += ns;
+        ++k;
+        spins = 0;
+        active = g < total;
+        if (active) load();
+      } else if (++spins > kStageSpins ||
+                 ((spins & 1023) == 0 && *(volatile int *)&ctl->bar_fail)) {
+        active = false;
+        ok = false;
+      }
+    }
+  }
+  if (!ok && !*(volatile int *)&ctl->bar_fail) mark_stage_timeout(ctl);
+  // the last fill of this stage: wait (bounded) for its bytes
+  if (st < ns && k > 0) ring_wait(ctl, &full[st], (k - 1) & 1u);
+}
+
+// One row of a streamed slice: the same arithmetic as phase_row (blocks in
+// slot order, three FMAs per block row entry, then phase_store), with the
+// slice's values, column indices and D block read from the ring stage.
+template <typename V, typename T>
+__device__ __forceinline__ void ring_row(const Phase &P, int row, int lane, int w, const V *sv,
+                                         const int *sc, const V *sd, const T *src, T *ybuf,
+                                         T *hat) {
+  // gathers in flight per batch (within the kernel's 128 registers)
+  constexpr int B = sizeof(T) == 8 ? 2 : 4;
+  const T *own = P.own_y ? ybuf : src;
+  const T *nbr = P.nbr_hat ? hat : ybuf;
+  T a0 = __ldcg(own + 3 * row), a1 = __ldcg(own + 3 * row + 1), a2 = __ldcg(own + 3 * row + 2);
+  for (int k0 = 0; k0 < w; k0 += B) {
+    int c[B];
+    T x[B][3];
+#pragma unroll
+    for (int j = 0; j < B; ++j) c[j] = (k0 + j < w) ? sc[(k0 + j) * 32 + lane] : -1;
+#pragma unroll
+    for (int j = 0; j < B; ++j)
+      if (c[j] >= 0) {
+        const T *xs = (c[j] < P.src_rows ? src : nbr) + 3 * c[j];
+        x[j][0] = __ldcg(xs);
+        x[j][1] = __ldcg(xs + 1);
+        x[j][2] = __ldcg(xs + 2);
+      }
+#pragma unroll
+    for (int j = 0; j < B; ++j)
+      if (c[j] >= 0) {
+        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + lane;
+        a0 = fma(-(T)b[0 * 32], x[j][0], a0); a0 = fma(-(T)b[1 * 32], x[j][1], a0);
+        a0 = fma(-(T)b[2 * 32], x[j][2], a0);
+        a1 = fma(-(T)b[3 * 32], x[j][0], a1); a1 = fma(-(T)b[4 * 32], x[j][1], a1);
+        a1 = fma(-(T)b[5 * 32], x[j][2], a1);
+        a2 = fma(-(T)b[6 * 32], x[j][0], a2); a2 = fma(-(T)b[7 * 32], x[j][1], a2);
+        a2 = fma(-(T)b[8 * 32], x[j][2], a2);
+      }
+  }
+  phase_store<V, T, false>(P, row, sd + lane, a0, a1, a2, ybuf, hat);
+}
+
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
 // launch. Consecutive steps are separated by a grid barrier, by a CTA
 // barrier (two single-slice steps on CTA 0), or by nothing at all inside a
 // run of staged steps, whose consumers wait for the values they read
 // (sentinel outputs, see is_sentinel). Vector loads go through
 // L2 because earlier steps of the same launch wrote them on other SMs.
-// Staged small steps read their matrix data from shared memory.
+// Staged small steps read their matrix data from shared memory; with a
+// ring (sp.ring_ns > 0) the last warp becomes the producer of the large
+// steps' slices and the other warps compute, synchronising among
+// themselves on a named barrier.
 template <typename V, typename T>
 __global__ void __launch_bounds__(coop_threads<T>(), 1)
 k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
@@ -821,11 +1011,26 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
            const T *src, T *ybuf, T *hat) {
   extern __shared__ __align__(128) unsigned char stage_smem[];
   __shared__ uint64_t stage_bar;
+  __shared__ uint64_t ring_full[kRingMax], ring_empty[kRingMax];
+  __shared__ int ring_w[kRingMax];
+  __shared__ unsigned int ring_seq[kRingMax];   // slice number a stage is filled with
   __shared__ StageEntry stage_tab[kMaxStage];
   __shared__ int stage_n;
   __shared__ T xch[sizeof(T) == 8 ? comp_groups<T>() : 1][3][32];   // FP64 component exchange
   if (ctl->done) return;
+  constexpr int NT = coop_threads<T>();
+  const bool ring = sp.ring_ns > 0;
+  const int ncw = ring ? NT / 32 - 1 : NT / 32;   // compute warps
+  const int nct = 32 * ncw;                       // compute threads
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   bool staged_ready = false;
+  if (ring && threadIdx.x == 0) {
+    for (int st = 0; st < sp.ring_ns; ++st) {
+      mbar_init(&ring_full[st], 1);
+      mbar_init(&ring_empty[st], 1);
+      ring_seq[st] = 0xffffffffu;
+    }
+  }
   if (sp.enabled) {
     const int2 cnt = sp.cnt[blockIdx.x];
     if (threadIdx.x == 0) {
@@ -834,8 +1039,10 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       mbar_expect_tx(&stage_bar, (uint32_t)cnt.y);
     }
     if (threadIdx.x < cnt.x) stage_tab[threadIdx.x] = sp.tab[(size_t)blockIdx.x * kMaxStage + threadIdx.x];
-    __syncthreads();
-    if (threadIdx.x < cnt.x) {
+  }
+  __syncthreads();
+  if (sp.enabled) {
+    if (threadIdx.x < stage_n) {
       const StageEntry e = stage_tab[threadIdx.x];
       const Phase P = ph.p[e.q];
       const int s = P.slice0 + e.j;
@@ -853,10 +1060,10 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
     // sentinels into the outputs of this CTA's staged rows; a grid barrier
     // separates them from every consumer
     const T sent = sentinel_value<T>();
-    for (int e = threadIdx.x >> 5; e < stage_n; e += coop_threads<T>() / 32) {
+    for (int e = warp; e < stage_n; e += NT / 32) {
       const StageEntry E = stage_tab[e];
       const Phase &P = ph.p[E.q];
-      const int r = 32 * E.j + (threadIdx.x & 31);
+      const int r = 32 * E.j + lane;
       if (r >= P.nrows) continue;
       const int row = P.row0 + r;
       if (P.to_y)
@@ -865,8 +1072,15 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         for (int k = 0; k < 3; ++k) st_relaxed(hat + 3 * row + k, sent);
     }
   }
-  constexpr int NT = coop_threads<T>();
-  const int stride = gridDim.x * NT;
+  unsigned char *ring_base = stage_smem + sp.ring_off;
+  if (ring && warp == NT / 32 - 1) {
+    // the producer warp (one lane per stage) leaves the CTA's barriers
+    // from here on
+    ring_produce<V>(ctl, sp, ring_base, ring_full, ring_empty, ring_w, ring_seq, off1, col1,
+                    val1, off2, col2, val2, dmat, (unsigned int)lane);
+    return;
+  }
+  const int stride = gridDim.x * nct;
   // Every thread acquires the completed bulk copies itself, with a bounded
   // wait, just before the grid barrier that precedes the first staged step
   // (the copies finished long before); the barrier's own CTA-wide sync
@@ -884,17 +1098,18 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
   bool run = true;
   if (first_staged == 0) {
     // every step is small: the sentinels need a grid barrier before any step
-    run = grid_barrier(ctl, copies_late());
+    run = grid_barrier(ctl, copies_late(), nct);
     staged_ready = run;
   }
+  unsigned int gseq = 0;   // ring slices of this CTA in the streamed steps so far
   for (int q = 0; run && q < ph.n; ++q) {
     if (ph.trace && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[q] = globaltimer();
     const Phase P = ph.p[q];
     const int *off = P.mat ? off2 : off1;
     const int *col = P.mat ? col2 : col1;
     const V *val = P.mat ? val2 : val1;
+    bool late = false;   // a ring wait of this warp ran out
     if (P.staged && sp.enabled) {
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
       if constexpr (sizeof(T) == 8) {
         // FP64: three warps per slice, one per row component. A small step
         // gives each SM one or two slices, and one warp's FP64 instructions
@@ -956,7 +1171,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
           if (valid && fin) st_relaxed(hat + 3 * row + c, a);
         }
       } else {
-        for (int e = warp; e < stage_n; e += NT / 32) {
+        for (int e = warp; e < stage_n; e += ncw) {
           const StageEntry E = stage_tab[e];
           if (E.q != q) continue;
           const int r = 32 * E.j + lane;
@@ -969,12 +1184,44 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
           staged_row<V, T>(P, P.row0 + r, lane, E.w, sv, sc, sd, src, ybuf, hat, ctl);
         }
       }
+    } else if (P.streamed && ring) {
+      // this CTA's slices j = blockIdx.x + t * grid come from the ring in
+      // order; compute warp w takes the slices whose number in the CTA's
+      // sequence is w modulo the compute warps
+      const int nsl = (P.nrows + 31) >> 5;
+      const int nq = (int)blockIdx.x < nsl ? (nsl - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+      const unsigned int ns = (unsigned int)sp.ring_ns;
+      for (int t = (warp - (int)(gseq % ncw) + ncw) % ncw; t < nq; t += ncw) {
+        const unsigned int g = gseq + t, st = g % ns;
+        // every lane acquires the fill itself; the warp goes on only if all did
+        const bool got = __all_sync(
+            0xffffffffu, ring_wait_slice(ctl, &ring_seq[st], g, &ring_full[st], (g / ns) & 1u));
+        if (!got) {
+          // the other waits of the run give up at once from here on
+          if (!*(volatile int *)&ctl->bar_fail) mark_stage_timeout(ctl);
+          late = true;
+          break;
+        }
+        const int j = blockIdx.x + t * gridDim.x;
+        const int r = 32 * j + lane;
+        const unsigned char *stage = ring_base + (size_t)st * sp.ring_stride;
+        const int w = ring_w[st];
+        if (r < P.nrows)
+          ring_row<V, T>(P, P.row0 + r, lane, w, reinterpret_cast<const V *>(stage),
+                         reinterpret_cast<const int *>(stage + w * 9 * 32 * sizeof(V)),
+                         reinterpret_cast<const V *>(stage + w * 9 * 32 * sizeof(V) +
+                                                     w * 32 * sizeof(int)),
+                         src, ybuf, hat);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ring_empty[st]);
+      }
+      gseq += nq;
     } else {
       // slice j of the step goes to CTA j % grid: the device numbering puts
       // a color's widest rows first, and contiguous chunks per CTA would
       // hand them all to the first CTAs, which every barrier then waits for
-      const int lane = threadIdx.x & 31, nsl = (P.nrows + 31) >> 5;
-      for (int j = (threadIdx.x >> 5) * gridDim.x + blockIdx.x; j < nsl; j += stride >> 5) {
+      const int nsl = (P.nrows + 31) >> 5;
+      for (int j = warp * gridDim.x + blockIdx.x; j < nsl; j += stride >> 5) {
         const int t = 32 * j + lane;
         if (t < P.nrows)
           phase_row<V, T, true>(P, P.row0 + t, P.slice0 + j, lane, off, col, val, dmat, src, ybuf,
@@ -985,15 +1232,17 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
     if (q + 1 < ph.n && P.flow_after && P.staged && ph.p[q + 1].staged && sp.enabled) {
       // data-ordered: the next step waits for the values it reads
     } else if (q + 1 < ph.n && P.local_after) {
-      __syncthreads();   // the next step reads this one's rows, all written by this CTA
+      cta_sync(nct);   // the next step reads this one's rows, all written by this CTA
     } else if (q + 1 < ph.n) {
       const bool before_staged = q + 1 == first_staged;
-      ok = grid_barrier(ctl, before_staged && copies_late());
+      ok = grid_barrier(ctl, late || (before_staged && copies_late()), nct);
       if (ok && before_staged) staged_ready = true;
+    } else if (late && !*(volatile int *)&ctl->bar_fail) {
+      mark_stage_timeout(ctl);
     }
     if (ok && ph.trace && q + 1 == ph.n) {
       // the end of the last phase: after every CTA finished it
-      ok = grid_barrier(ctl);
+      ok = grid_barrier(ctl, false, nct);
       if (ok && blockIdx.x == 0 && threadIdx.x == 0) ctl->phase_ns[ph.n] = globaltimer();
     }
     if (!ok) break;

@@ -28,7 +28,7 @@ class Options(C.Structure):
                 ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
                 ("factor_on_device", C.c_int), ("mixed_scheme", C.c_int),
                 ("ru_delta", C.c_double), ("stage_small_steps", C.c_int),
-                ("coloring", C.c_int)]
+                ("coloring", C.c_int), ("stream_large_steps", C.c_int)]
 
 
 class Result(C.Structure):
@@ -53,11 +53,13 @@ class Stats(C.Structure):
                 ("launches_per_iter", C.c_int), ("last_launches", C.c_longlong),
                 ("factor_ms", C.c_double), ("analyze_ms", C.c_double),
                 ("alg_bytes_spmv", C.c_double * 2), ("alg_bytes_ilu", C.c_double * 2),
-                ("alg_bytes_iter", C.c_double * 2)]
+                ("alg_bytes_iter", C.c_double * 2), ("ring_stages", C.c_int * 2),
+                ("ring_stage_bytes", C.c_int * 2), ("apply_smem_bytes", C.c_int * 2)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
-        for k in ("alg_bytes_spmv", "alg_bytes_ilu", "alg_bytes_iter"):
+        for k in ("alg_bytes_spmv", "alg_bytes_ilu", "alg_bytes_iter", "ring_stages",
+                  "ring_stage_bytes", "apply_smem_bytes"):
             d[k] = list(d[k])
         return d
 
@@ -134,7 +136,8 @@ class GbIlu:
     def __init__(self, precision="fp64", device=0, use_graph=True, absolute=False,
                  timeout_ms=0.0, inner_tol=1e-1, inner_maxit=500, max_outer=30,
                  verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
-                 ru_delta=0.1, stage_small_steps=True, coloring="parity"):
+                 ru_delta=0.1, stage_small_steps=True, coloring="parity",
+                 stream_large_steps=False):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -153,6 +156,7 @@ class GbIlu:
         o.ru_delta = ru_delta
         o.stage_small_steps = int(stage_small_steps)
         o.coloring = {"parity": 0, "natural": 1}[coloring]
+        o.stream_large_steps = int(stream_large_steps)
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:

@@ -101,6 +101,12 @@ typedef struct {
                          connection) moved to the end of the order -- which
                          leaves one small color on a grid with faults;
                          1: first-fit greedy in natural row order */
+  int stream_large_steps; /* 1: in the single-launch apply one warp per CTA
+                         streams the large color steps' matrix slices into a
+                         shared-memory ring with bulk copies (running ahead
+                         across barriers) and the others compute from it;
+                         0 (default): every warp loads its own rows (same
+                         results) */
 } gbilu_options;
 
 typedef struct {
@@ -145,6 +151,12 @@ typedef struct {
   double alg_bytes_spmv[2];
   double alg_bytes_ilu[2];
   double alg_bytes_iter[2];
+  /* the forward single-launch apply, [0] FP64 / [1] FP32 (0 when that
+   * precision is not set up): stages and bytes per stage of the ring that
+   * streams the large color steps, dynamic shared memory per CTA */
+  int ring_stages[2];
+  int ring_stage_bytes[2];
+  int apply_smem_bytes[2];
 } gbilu_stats;
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,

@@ -375,14 +375,14 @@ def test_staging_off_bit_identical(case, precision):
 
 
 def test_partly_staged_500k_bit_identical(built_lib):
-    """A 500k-cell system whose color 2 (17135 rows) is above the staging
-    limit: staged runs and global-memory steps mixed in one apply, against
-    one launch per color step."""
+    """A 500k-cell system whose color 2 (17135 rows with the natural-order
+    coloring) is above the staging limit: staged runs and global-memory
+    (streamed) steps mixed in one apply, against one launch per color step."""
     s = generate(100, 100, 50, sigma=1.5, inactive_frac=0.05, fault_frac=0.01, seed=1)
     p = np.random.default_rng(10).standard_normal(s.n)
     runs = []
     for mode in (1, 0):
-        with GbIlu(device=0, sweep_mode=mode) as h:
+        with GbIlu(device=0, sweep_mode=mode, coloring="natural") as h:
             h.analyze(s.rowptr, s.colind).factor(s.vals)
             x, r = h.solve(s.b, tol=1e-6, maxit=500)
             assert r.status == 0
@@ -390,3 +390,50 @@ def test_partly_staged_500k_bit_identical(built_lib):
     (x1, k1, z1, t1), (x2, k2, z2, t2) = runs
     assert k1 == k2 and np.array_equal(x1, x2)
     assert np.array_equal(z1, z2) and np.array_equal(t1, t2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_off_bit_identical(case, precision):
+    """The large color steps streamed through the shared-memory ring by a
+    producer warp give the same bits as every warp loading its own rows."""
+    s, P, g = case
+    p = np.random.default_rng(9).standard_normal(s.n)
+    runs = []
+    for ring in (True, False):
+        with GbIlu(device=0, precision=precision, stream_large_steps=ring) as h:
+            h.analyze(s.rowptr, s.colind).factor(s.vals)
+            x, r = h.solve(s.b, tol=1e-8, maxit=500)
+            runs.append((x, r.half_iters, h.ilu_apply(p), h.ilu_apply(p, True)))
+    (x1, k1, z1, t1), (x2, k2, z2, t2) = runs
+    assert k1 == k2 and np.array_equal(x1, x2)
+    assert np.array_equal(z1, z2) and np.array_equal(t1, t2)
+
+
+@pytest.mark.parametrize("coloring", ["parity", "natural"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_500k_bit_identical(built_lib, precision, coloring):
+    """The 500k-cell system: the single-launch apply with its streamed large
+    steps, without the ring, and one launch per color step give the same
+    bits (forward and transposed applies, FP64; solves in both precisions);
+    the FP64 apply matches the oracle to the kernel tolerance."""
+    s = make_config("c2_100x100x50")
+    p = np.random.default_rng(12).standard_normal(s.n)
+    runs = []
+    for kw in (dict(stream_large_steps=True), dict(stream_large_steps=False),
+               dict(sweep_mode=0)):
+        with GbIlu(device=0, precision=precision, coloring=coloring, **kw) as h:
+            h.analyze(s.rowptr, s.colind).factor(s.vals)
+            if kw.get("stream_large_steps"):
+                st = h.stats()
+                f = 1 if precision == "mixed" else 0
+                assert st["ring_stages"][f] >= 4 and st["apply_smem_bytes"][f] > 0
+            x, r = h.solve(s.b, tol=1e-4, maxit=500)
+            assert r.status == 0
+            runs.append((x, r.half_iters, h.ilu_apply(p), h.ilu_apply(p, True)))
+    for x2, k2, z2, t2 in runs[1:]:
+        assert k2 == runs[0][1] and np.array_equal(x2, runs[0][0])
+        assert np.array_equal(z2, runs[0][2]) and np.array_equal(t2, runs[0][3])
+    if precision == "fp64":
+        P = Prepared(s, coloring=coloring)
+        assert rel(runs[0][2], P.ilu_apply(p)) < KERNEL_TOL
+        assert rel(runs[0][3], P.ilu_apply(p, True)) < KERNEL_TOL
