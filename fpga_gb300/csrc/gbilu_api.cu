@@ -275,7 +275,13 @@ int coop_grid(Handle *h) {
 // kStageBudget bytes or kMaxStage entries. The large steps' ring takes the
 // shared memory left after the staged slices.
 constexpr int kStageBudget = 160 * 1024;
-constexpr int kRingMin = 4;   // fewer ring stages than this: no ring
+// A ring of fewer stages than this leaves compute warps waiting for a
+// stage (measured: the FP64 apply, 8 stages of 21.7 KB for 15 compute
+// warps, 82 -> 118 us): no ring.
+#ifndef GBILU_RING_MIN
+#define GBILU_RING_MIN 12
+#endif
+constexpr int kRingMin = GBILU_RING_MIN;
 
 // Bytes of one slice's [values | column indices | D block] in shared memory.
 template <typename V>
@@ -333,9 +339,17 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
   const long long ring_off = (most + 127) / 128 * 128;
   long long stride = 0;
   bool any_large = false;
+  // Only a large step that follows another step is streamed: its first
+  // stages fill while the steps before it run. The first step of the
+  // launch gains nothing from the ring (measured: FP32 L sweep of the
+  // 500k-cell system 16.3 us from global memory, 21.2 us streamed).
+  auto streamable = [&](int q) {
+    const Phase &P = pl.p[q];
+    return q > 0 && !P.staged && P.nrows > kSmallRows;
+  };
   for (int q = 0; q < pl.n; ++q) {
     const Phase &P = pl.p[q];
-    if (P.staged || P.nrows <= kSmallRows) continue;
+    if (!streamable(q)) continue;
     any_large = true;
     const int nsl = (P.nrows + kSliceRows - 1) / kSliceRows;
     for (int j = 0; j < nsl; ++j)
@@ -343,11 +357,17 @@ int build_stage_plan(Handle *h, int f, int t, int grid) {
   }
   stride = (stride + 127) / 128 * 128;
   const long long avail = (long long)optin - (long long)fa.sharedSizeBytes - ring_off;
-  const int ns = (stride > 0 && avail > 0) ? (int)std::min<long long>(kRingMax, avail / stride) : 0;
+// Stages of the FP32 ring: 12 is the best of 6..16 on the 500k-cell apply
+// (a larger ring leaves less L1 for the large steps that read global
+// memory: 8 stages 45.4 us, 12 41.9 us, 16 45.5 us)
+#ifndef GBILU_RING_STAGES
+#define GBILU_RING_STAGES 12
+#endif
+  const int ns = (stride > 0 && avail > 0)
+                     ? (int)std::min<long long>(GBILU_RING_STAGES, avail / stride) : 0;
   const bool ring = h->opt.stream_large_steps && any_large && ns >= kRingMin;
   if (ring)
-    for (int q = 0; q < pl.n; ++q)
-      pl.p[q].streamed = !pl.p[q].staged && pl.p[q].nrows > kSmallRows;
+    for (int q = 0; q < pl.n; ++q) pl.p[q].streamed = streamable(q);
   const long long dyn = ring ? ring_off + ns * stride : most;
   if (dyn > 0) {
     CK(cudaFuncSetAttribute(k_ilu_coop<V, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,

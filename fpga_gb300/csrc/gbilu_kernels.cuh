@@ -240,8 +240,10 @@ constexpr int kBatch = GBILU_BATCH;   // blocks whose loads are in flight togeth
 #endif
 constexpr int kBatch64 = GBILU_BATCH64;   // the same for FP64 values
 
-// Loads of vectors that other CTAs of the same kernel wrote go through L2
-// (ld.global.cg): the per-SM L1 is not coherent inside one launch.
+// Vector loads: CG = through L2 only (ld.global.cg), else through L1. The
+// per-SM L1 is not coherent inside one launch; loads of values that other
+// SMs may still be writing go through L2 (the small steps poll with relaxed
+// gpu-scope loads instead).
 template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p) {
   if (CG) return __ldcg(p);
   return *p;
@@ -860,6 +862,22 @@ __device__ __forceinline__ void group_sync(int g) {
   asm volatile("bar.sync %0, 96;" ::"r"(1 + g) : "memory");
 }
 
+#ifndef GBILU_LARGE_CACHED
+#define GBILU_LARGE_CACHED 1
+#endif
+// Vector loads of the large steps go through L1. Every large step follows a
+// grid barrier whose acquire (ld.acquire.gpu, then the CTA barrier) orders
+// the earlier steps' writes from other SMs before these loads, and no row a
+// large step reads is written during it (rows of one color are not
+// coupled), so the SM's L1 cannot serve a stale value; the three components
+// of a neighbour and neighbours shared by nearby rows then cost one L2
+// sector fetch instead of one per load.
+constexpr bool kLargeCached = GBILU_LARGE_CACHED != 0;
+template <typename T> __device__ __forceinline__ T ldl(const T *p) {
+  if (kLargeCached) return __ldca(p);
+  return __ldcg(p);
+}
+
 // Bounded mbarrier phase wait of the ring. Gives up after kStageSpins
 // polls, or early once another wait of the run failed. A parity wait only
 // tells the current phase of a barrier from the one before it, so a waiter
@@ -964,7 +982,7 @@ __device__ __forceinline__ void ring_row(const Phase &P, int row, int lane, int 
   constexpr int B = sizeof(T) == 8 ? 2 : 4;
   const T *own = P.own_y ? ybuf : src;
   const T *nbr = P.nbr_hat ? hat : ybuf;
-  T a0 = __ldcg(own + 3 * row), a1 = __ldcg(own + 3 * row + 1), a2 = __ldcg(own + 3 * row + 2);
+  T a0 = ldl(own + 3 * row), a1 = ldl(own + 3 * row + 1), a2 = ldl(own + 3 * row + 2);
   for (int k0 = 0; k0 < w; k0 += B) {
     int c[B];
     T x[B][3];
@@ -974,9 +992,9 @@ __device__ __forceinline__ void ring_row(const Phase &P, int row, int lane, int 
     for (int j = 0; j < B; ++j)
       if (c[j] >= 0) {
         const T *xs = (c[j] < P.src_rows ? src : nbr) + 3 * c[j];
-        x[j][0] = __ldcg(xs);
-        x[j][1] = __ldcg(xs + 1);
-        x[j][2] = __ldcg(xs + 2);
+        x[j][0] = ldl(xs);
+        x[j][1] = ldl(xs + 1);
+        x[j][2] = ldl(xs + 2);
       }
 #pragma unroll
     for (int j = 0; j < B; ++j)
@@ -1224,8 +1242,8 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       for (int j = warp * gridDim.x + blockIdx.x; j < nsl; j += stride >> 5) {
         const int t = 32 * j + lane;
         if (t < P.nrows)
-          phase_row<V, T, true>(P, P.row0 + t, P.slice0 + j, lane, off, col, val, dmat, src, ybuf,
-                                hat);
+          phase_row<V, T, !kLargeCached>(P, P.row0 + t, P.slice0 + j, lane, off, col, val, dmat,
+                                         src, ybuf, hat);
       }
     }
     bool ok = true;

@@ -423,10 +423,11 @@ def test_ring_500k_bit_identical(built_lib, precision, coloring):
                dict(sweep_mode=0)):
         with GbIlu(device=0, precision=precision, coloring=coloring, **kw) as h:
             h.analyze(s.rowptr, s.colind).factor(s.vals)
-            if kw.get("stream_large_steps"):
+            if kw.get("stream_large_steps") and precision == "mixed":
+                # the FP32 apply streams its second large step (FP64 slices
+                # leave too few stages for a ring)
                 st = h.stats()
-                f = 1 if precision == "mixed" else 0
-                assert st["ring_stages"][f] >= 4 and st["apply_smem_bytes"][f] > 0
+                assert st["ring_stages"][1] >= 12 and st["apply_smem_bytes"][1] > 0
             x, r = h.solve(s.b, tol=1e-4, maxit=500)
             assert r.status == 0
             runs.append((x, r.half_iters, h.ilu_apply(p), h.ilu_apply(p, True)))
