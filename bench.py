@@ -251,6 +251,7 @@ def gpu_bench(args, world, rank, local):
         ms, by, la = g.bench_kernel(name, reps=20)
         kern[name] = {"ms": ms, "alg_bytes": by, "launches": la, "gbs": by / ms / 1e6}
     trace = {"fp64": g.ilu_trace(fp32=False), "fp32": g.ilu_trace(fp32=True)}
+    budget = iteration_budget(g, g64, st, b_dev, x_dev, local)
     it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
     solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
     traffic = None
@@ -295,6 +296,8 @@ def gpu_bench(args, world, rank, local):
                "solve_frac_of_peak": solve_gbs / peak if solve_gbs else None,
                "kernels": kern,
                "ilu_phases_rows_us": trace,
+               "iteration_budget": budget,
+               "analysis": analysis_timing(s, local),
                "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": 2 * n * 8,
                        "d2h_bytes_per_step": n * 8},
                "gpu_launches": int(launches),
@@ -304,6 +307,77 @@ def gpu_bench(args, world, rank, local):
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
+
+
+FP64_FMA_LANES_PER_CLK_SM = 1.68   # measured on GB300 (independent DFMA chains)
+SM_CLOCK_HZ = 2.07e9
+
+
+def iteration_budget(g, g64, st, b_dev, x_dev, local):
+    """Where one BiCGSTAB iteration's time goes: every kernel of the
+    iteration timed alone (back to back, CUDA events), beside its HBM floor
+    (algorithmic bytes at the measured copy peak) and, for FP64, its FP64
+    floor (DFMA count at the measured FP64 rate); and the measured time per
+    iteration of whole solves (the slope between maxit 4 and 12, tol 0)."""
+    import torch
+    peak, _ = peaks()
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    fma_rate = FP64_FMA_LANES_PER_CLK_SM * sms * SM_CLOCK_HZ
+    n, nb, nnzb = 3 * st["nb"], st["nb"], st["nnzb"]
+    nlu = st["nnzb_lower"] + st["nnzb_upper"]
+    # DFMA per launch (FP64): SpMV 9 per block (+ the fused dots), apply 9
+    # per L, U and D block, update_s 2n, update_r 5n, update_p 2n
+    fmas = {"ilu": 9 * (nlu + nb), "spmv_alpha": 9 * nnzb + n, "spmv_omega": 9 * nnzb + 2 * n,
+            "update_s": 2 * n, "update_r": 5 * n, "update_p": 2 * n}
+    out = {}
+    for prec, suf in (("fp64", "64"), ("fp32", "32")):
+        rows = {}
+        for name, count in (("ilu", 2), ("spmv_alpha", 1), ("spmv_omega", 1), ("update_s", 1),
+                            ("update_r", 1), ("update_p", 1)):
+            ms, by, la = g.bench_kernel(name + suf, reps=20)
+            r = {"per_iter": count, "us": ms * 1e3, "alg_bytes": by,
+                 "hbm_floor_us": by / (peak * 1e9) * 1e6}
+            if prec == "fp64":
+                r["fp64_floor_us"] = fmas[name] / fma_rate * 1e6
+            rows[name] = r
+        tot = sum(r["us"] * r["per_iter"] for r in rows.values())
+        out[prec] = {"kernels": rows, "sum_us": tot,
+                     "hbm_floor_sum_us": sum(r["hbm_floor_us"] * r["per_iter"] for r in rows.values())}
+        if prec == "fp64":
+            out[prec]["fp64_floor_sum_us"] = sum(r["fp64_floor_us"] * r["per_iter"]
+                                                 for r in rows.values())
+    # measured per-iteration time of the FP64 graph loop
+    t = {}
+    for m in (4, 12):
+        ms = []
+        for _ in range(3):
+            x_dev.zero_()
+            ms.append(g64.solve_device(b_dev.data_ptr(), x_dev.data_ptr(), 0.0, m).device_ms)
+        t[m] = statistics.median(ms)
+    out["fp64"]["measured_us_per_iter"] = (t[12] - t[4]) / 8 * 1e3
+    out["fp64"]["overhead_us_per_iter"] = out["fp64"]["measured_us_per_iter"] - out["fp64"]["sum_us"]
+    return out
+
+
+def analysis_timing(s, local):
+    """Analysis (coloring, ordering, device layout and upload) and ILU0
+    factorization of the headline system, timed separately: host-only
+    analysis, analysis of a device handle, host factorization (with the
+    upload), device factorization."""
+    from fpga_gb300 import GbIlu
+    out = {}
+    with GbIlu(device=-1) as h:
+        h.analyze(s.rowptr, s.colind)
+        out["analyze_ms_host_only"] = h.stats()["analyze_ms"]
+    for dev in (False, True):
+        with GbIlu(device=local, factor_on_device=dev) as h:
+            h.analyze(s.rowptr, s.colind)
+            h.factor(s.vals)
+            h.factor(s.vals)          # the second factorization (warm)
+            st = h.stats()
+            out["analyze_ms_device_handle"] = st["analyze_ms"]
+            out["factor_ms_device" if dev else "factor_ms_host"] = st["factor_ms"]
+    return out
 
 
 def cpu_baseline(s, tol, maxit):
@@ -495,11 +569,18 @@ def mixed_adjoint_2m(local):
         # inside the timed region (b and x0; g, and x for dL/dA)
         res[prec] = {"forward_ms": fw, "adjoint_ms": bw, "ratio": bw / fw,
                      "adjoint_ms_full": bw_full, "ratio_full": bw_full / fw,
+                     "analyze_ms": g.stats()["analyze_ms"],
+                     "factor_ms_host": g.stats()["factor_ms"],
                      "forward_status": r.status, "adjoint_status": ra.status,
                      "forward_true_relres": r.true_relres, "adjoint_true_relres": ra.true_relres,
                      "device_bytes_handle": g.stats()["device_bytes"],
                      "device_bytes_measured": free0 - free1}
         g.close()
+    with GbIlu(device=local, precision="mixed", factor_on_device=True) as g:
+        g.analyze(s.rowptr, s.colind)
+        g.factor(s.vals)
+        g.factor(s.vals)
+        res["mixed"]["factor_ms_device"] = g.stats()["factor_ms"]
     res["lambda_rel_err_vs_fp64"] = float(np.linalg.norm(grads["mixed"][0] - grads["fp64"][0]) /
                                           np.linalg.norm(grads["fp64"][0]))
     res["dA_rel_err_vs_fp64"] = float(np.linalg.norm(grads["mixed"][1] - grads["fp64"][1]) /

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace gbilu {
@@ -1025,6 +1026,32 @@ int solve_mixed(Handle *h, bool transpose, double tol, int maxit, gbilu_result *
 }  // namespace
 }  // namespace gbilu
 
+namespace gbilu {
+namespace {
+// One of the iteration's kernels for gbilu_bench_kernel (kind 4: SpMV with
+// the alpha dot, 5: SpMV with the omega dots, 6-8: update_s/r/p).
+template <typename V, typename T>
+void iter_kernel(Handle *h, int kind, const Ops<V, T> &o, int n, int g, int gr, int &l) {
+  Vecs<T> &w = *o.vec;
+  if (kind == 4) {
+    spmv<V, T, SPMV_ALPHA>(h, h->st, o, w.p.p, w.v.p, w.rt.p, l);
+  } else if (kind == 5) {
+    spmv<V, T, SPMV_OMEGA>(h, h->st, o, w.p.p, w.t.p, w.s.p, l);
+  } else if (kind == 6) {
+    k_update_s<T><<<gr, kThreads, 0, h->st>>>(h->ctl.p, n, w.r.p, w.v.p, w.s.p, h->partials.p);
+    ++l;
+  } else if (kind == 7) {
+    k_update_r<T><<<gr, kThreads, 0, h->st>>>(h->ctl.p, n, w.x.p, w.ph.p, w.sh.p, w.s.p, w.t.p,
+                                              w.rt.p, w.r.p, h->partials.p);
+    ++l;
+  } else {
+    k_update_p<T><<<g, kThreads, 0, h->st>>>(h->ctl.p, n, w.r.p, w.v.p, w.p.p, 0ull);
+    ++l;
+  }
+}
+}  // namespace
+}  // namespace gbilu
+
 using namespace gbilu;
 
 extern "C" {
@@ -1442,6 +1469,33 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   return GBILU_OK;
 }
 
+int gbilu_dot_check(void *handle, int n, const float *x, const float *y, double *dot_df,
+                    double *dot_fp64) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h || n <= 0 || !x || !y) return GBILU_BAD_INPUT;
+  if (!h->analyzed) return h->fail(GBILU_NOT_READY, "gbilu_analyze has not been called");
+  if (h->opt.device < 0) return h->fail(GBILU_NO_DEVICE, "host-only handle cannot run the check");
+  if (!h->with_32) return h->fail(GBILU_BAD_INPUT, "the FP32 dot check needs GBILU_MIXED");
+  if (n > 3 * h->an.nb) return h->fail(GBILU_BAD_INPUT, "n exceeds 3*nb");
+  CK(cudaSetDevice(h->opt.device));
+  Ctl *c = h->ctl.p + 1;   // the spare control block
+  k_ctl_init<<<1, 32, 0, h->st>>>(c, 0.0, 0, 0, 0ull);
+  CK(cudaMemcpyAsync(h->v32.r.p, x, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->v32.s.p, y, n * sizeof(float), cudaMemcpyHostToDevice, h->st));
+  double out[2];
+  for (int mode = 0; mode < 2; ++mode) {
+    k_dot_check<<<reduce_grid(h, n), kThreads, 0, h->st>>>(c, n, h->v32.r.p, h->v32.s.p, mode,
+                                                            h->partials.p);
+    CK(cudaMemcpyAsync(h->h_ctl, c, sizeof(Ctl), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    out[mode] = h->h_ctl->dots[0];
+  }
+  CK(last_error(h));
+  if (dot_df) *dot_df = out[0];
+  if (dot_fp64) *dot_fp64 = out[1];
+  return GBILU_OK;
+}
+
 int gbilu_wait_probe(void *handle, int mode, int *bar_fail, int *status, double *ms) {
   Handle *h = static_cast<Handle *>(handle);
   if (!h || (mode != 0 && mode != 1)) return GBILU_BAD_INPUT;
@@ -1536,8 +1590,9 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   if (!h) return GBILU_BAD_INPUT;
   int rc = check_solve_ready(h);
   if (rc) return rc;
-  if (which < 0 || which > 3 || reps <= 0) return h->fail(GBILU_BAD_INPUT, "bad kernel id or reps");
-  if (which >= 2 && !h->with_32) return h->fail(GBILU_BAD_INPUT, "FP32 kernels need GBILU_MIXED");
+  if (which < 0 || which > 13 || reps <= 0) return h->fail(GBILU_BAD_INPUT, "bad kernel id or reps");
+  const bool fp32 = which == 2 || which == 3 || which >= 9;
+  if (fp32 && !h->with_32) return h->fail(GBILU_BAD_INPUT, "FP32 kernels need GBILU_MIXED");
   CK(cudaSetDevice(h->opt.device));
   gbilu_stats st;
   gbilu_get_stats(h, &st);
@@ -1553,8 +1608,30 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   }
   CK(cudaMemcpyAsync(h->v64.p.p, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   if (h->with_32) k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0, h->v64.p.p, h->v32.p.p);
+  if (which >= 4) {
+    // every work vector of the iteration holds the same data, so that the
+    // dots are nonzero and no kernel stops the run
+    Vecs<double> &w = h->v64;
+    for (DevBuf<double> *b : {&w.x, &w.r, &w.rt, &w.ph, &w.v, &w.s, &w.sh, &w.t, &w.y})
+      CK(cudaMemcpyAsync(b->p, w.p.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    if (h->with_32) {
+      Vecs<float> &f = h->v32;
+      for (DevBuf<float> *b : {&f.x, &f.r, &f.rt, &f.ph, &f.v, &f.s, &f.sh, &f.t, &f.y})
+        CK(cudaMemcpyAsync(b->p, f.p.p, n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+    }
+  }
+  // the iteration's other kernels (4-8 FP64, 9-13 FP32): the SpMV with the
+  // alpha dot, the SpMV with the omega dots, update_s, update_r, update_p,
+  // with solver scalars that never stop the run
+  const int kind = which >= 9 ? which - 5 : which;
+  if (which >= 4) k_ctl_bench<<<1, 32, 0, h->st>>>(h->ctl.p);
+  const int gr = reduce_grid(h, n);
   auto run = [&](int &l) {
-    if (which == 0) {
+    if (which >= 9) {
+      iter_kernel<float, float>(h, kind, make_ops<float, float>(h, false), n, g, gr, l);
+    } else if (which >= 4) {
+      iter_kernel<double, double>(h, kind, make_ops<double, double>(h, false), n, g, gr, l);
+    } else if (which == 0) {
       Ops<double, double> o = make_ops<double, double>(h, false);
       spmv<double, double, SPMV_PLAIN>(h, h->st, o, h->v64.p.p, h->v64.v.p, nullptr, l);
     } else if (which == 1) {
@@ -1579,7 +1656,18 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->e0, h->e1));
   if (avg_ms) *avg_ms = ms / reps;
-  if (alg_bytes) *alg_bytes = (which == 0 || which == 2) ? st.alg_bytes_spmv[which / 2] : st.alg_bytes_ilu[which / 2];
+  if (alg_bytes) {
+    const double sx = fp32 ? 4.0 : 8.0, nn = n;
+    const int p = fp32 ? 1 : 0;
+    // each operand read or written once: the SpMV plus its dot operand
+    // (alpha: rt; omega: s), update_s r, v -> s; update_r x, p^, s^, s, t,
+    // rt -> x, r; update_p r, v, p -> p
+    const double by[5] = {st.alg_bytes_spmv[p] + nn * sx, st.alg_bytes_spmv[p] + nn * sx,
+                          3 * nn * sx, 8 * nn * sx, 4 * nn * sx};
+    *alg_bytes = which >= 4 ? by[kind - 4]
+                            : (which == 0 || which == 2) ? st.alg_bytes_spmv[which / 2]
+                                                         : st.alg_bytes_ilu[which / 2];
+  }
   if (launches_out) *launches_out = launches / reps;
   return GBILU_OK;
 }

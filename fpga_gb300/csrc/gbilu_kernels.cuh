@@ -206,6 +206,21 @@ __global__ void k_ctl_init(Ctl *c, double tol, int absolute, int maxit,
   }
 }
 
+// Solver scalars for timing the iteration's kernels one at a time: unit
+// rho, alpha, omega, beta, a zero bound and no iteration limit, so that no
+// kernel stops the run.
+__global__ void k_ctl_bench(Ctl *c) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    c->rho = c->alpha = c->omega = c->beta = 1.0;
+    c->bound = 0.0;
+    c->maxit = 0x7fffffff;
+    c->half = 0;
+    c->k = 0;
+    c->done = 0;
+    c->ru_mode = 0;
+  }
+}
+
 // Steps 0/1 of the PROGRAM (solver_pkg.vhd:122-123, solver.vhd:887-911):
 // r = b - A x0, rho = ||r||^2, the "already solved" test and the absolute
 // stopping bound. MODE 0: r = b - A x (vals/x given); MODE 1: r = b (x0 = 0,
@@ -1596,6 +1611,24 @@ k_norm2(Ctl *ctl, int n, const double *__restrict__ v, double *partials) {
   double vv[1] = {d}, tot[1];
   if (grid_sum<1>(vv, partials, &ctl->counter[5], tot) && threadIdx.x == 0)
     ctl->dots[0] = tot[0];
+}
+
+// (x, y) of FP32 vectors into ctl->dots[0] two ways: mode 0 as the FP32
+// kernels of the solve accumulate their dots (a double-float sum per thread
+// on the FP32 pipe, FP64 across threads), mode 1 with an FP64 sum per
+// thread (a diagnostic of the first against the second).
+__global__ void __launch_bounds__(kThreads)
+k_dot_check(Ctl *ctl, int n, const float *__restrict__ x, const float *__restrict__ y, int mode,
+            double *partials) {
+  double d = 0.0;
+  DF f = {0.f, 0.f};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    if (mode == 0) df_add_prod(f, x[i], y[i]);
+    else d += (double)x[i] * (double)y[i];
+  }
+  if (mode == 0) d = df_value(f);
+  double v[1] = {d}, tot[1];
+  if (grid_sum<1>(v, partials, &ctl->counter[5], tot) && threadIdx.x == 0) ctl->dots[0] = tot[0];
 }
 
 // dA[src[k]] = -lambda_i x_j^T for the blocks k of permuted row i

@@ -109,6 +109,8 @@ def load():
                                 C.POINTER(Result)]
     L.gbilu_adjoint_device.argtypes = [VP, VP, VP, VP, VP, C.c_double, C.c_int,
                                        C.POINTER(Result)]
+    L.gbilu_dot_check.argtypes = [VP, C.c_int, VP, VP, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
     L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
     L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
@@ -282,12 +284,25 @@ class GbIlu:
                                                 C.byref(res)))
         return res
 
+    def dot_check(self, x, y):
+        """(x, y) of two float32 vectors on the device: (double-float
+        accumulation as in the mixed solve, FP64 accumulation)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        a, b = C.c_double(), C.c_double()
+        self._check(self.L.gbilu_dot_check(self.h, x.size, x.ctypes.data, y.ctypes.data,
+                                           C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def stats(self):
         s = Stats()
         self._check(self.L.gbilu_get_stats(self.h, C.byref(s)))
         return s.as_dict()
 
-    KERNELS = {"spmv64": 0, "ilu64": 1, "spmv32": 2, "ilu32": 3}
+    KERNELS = {"spmv64": 0, "ilu64": 1, "spmv32": 2, "ilu32": 3,
+               "spmv_alpha64": 4, "spmv_omega64": 5, "update_s64": 6, "update_r64": 7,
+               "update_p64": 8, "spmv_alpha32": 9, "spmv_omega32": 10, "update_s32": 11,
+               "update_r32": 12, "update_p32": 13}
 
     def ilu_trace(self, fp32=False, transpose=False):
         """[(rows, microseconds)] per color step of one single-launch ILU apply."""

@@ -193,6 +193,15 @@ int gbilu_get_ordering(void *handle, int *ncolors, int *color, int *perm,
  * bicgstab_utils.cpp:93-129). */
 int gbilu_wait_probe(void *handle, int mode, int *bar_fail, int *status, double *ms);
 
+/* Diagnostic of the mixed mode's dot products: (x, y) of two FP32 host
+ * vectors of length n (n <= 3*nb) computed on the device as the FP32
+ * kernels of a mixed solve accumulate their dots (*dot_df: an error-free
+ * double-float sum per thread on the FP32 pipe, FP64 across threads) and
+ * with FP64 sums per thread (*dot_fp64). Needs GBILU_MIXED. No counterpart
+ * in the reference, whose dots are FP64. */
+int gbilu_dot_check(void *handle, int n, const float *x, const float *y, double *dot_df,
+                    double *dot_fp64);
+
 /* The numbering of the device vectors and sliced layouts: order[d] = input
  * row held at device row d. It keeps perm's color ranges and each color's
  * leading rows with a higher-colored neighbour, and inside each of these
@@ -266,8 +275,10 @@ int gbilu_get_stats(void *handle, gbilu_stats *stats);
 
 /* Times one kernel family on the handle's stream with CUDA events, reps
  * applications back to back on the factored system: which = 0 SpMV FP64,
- * 1 ILU apply FP64 (all colors), 2 SpMV FP32, 3 ILU apply FP32 (2/3 need
- * GBILU_MIXED). Returns the average device ms per application, its
+ * 1 ILU apply FP64 (all colors), 2 SpMV FP32, 3 ILU apply FP32; the other
+ * kernels of one iteration, 4-8 in FP64 and 9-13 in FP32: SpMV with the
+ * alpha dot, SpMV with the omega dots, update_s, update_r, update_p (FP32
+ * ids need GBILU_MIXED). Returns the average device ms per application, its
  * algorithmic bytes and the kernel launches per application. The
  * counterpart of the reference's kernel timing around clEnqueueTask
  * (fpga_functions_bicgstab.cpp:1305-1325), per kernel instead of per run. */
