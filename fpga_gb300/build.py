@@ -19,7 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libgbilu.so")
-SOURCES = ["gbilu_host.cpp", "gbilu_api.cu", "gbilu_noalloc.cu", "gbilu_fpga_compat.cpp"]
+SOURCES = ["gbilu_host.cpp", "gbilu_api.cu", "gbilu_noalloc.cu", "gbilu_fpga_compat.cpp",
+           "gbilu_fpga_export.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -2,6 +2,7 @@
 // device memory, the BiCGSTAB launch sequence, its CUDA graph (a device-side
 // while loop), iterative refinement for the mixed mode and the adjoint.
 #include "gbilu.h"
+#include "gbilu_fpga_export.hpp"
 #include "gbilu_host.hpp"
 #include "gbilu_kernels.cuh"
 
@@ -103,6 +104,7 @@ struct Handle {
   DevBuf<int> pdiag, bad;
   DevBuf<double> pbuf, vals_in, dinvp;
   bool host_factors_stale = false;
+  std::unique_ptr<FpgaExport> fpga;        // the last gbilu_fpga_export (sizes query)
   DevBuf<Ctl> ctl;                         // [0] main run, [1] refinement residual
   Ctl *h_ctl = nullptr;                    // pinned mirror
   bool with_t = false, with_32 = false;
@@ -1117,6 +1119,7 @@ int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind) {
   if (!h) return GBILU_BAD_INPUT;
   auto t0 = std::chrono::steady_clock::now();
   h->analyzed = h->factored = false;
+  h->fpga.reset();
   if (h->opt.coloring != 0 && h->opt.coloring != 1)
     return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: coloring must be 0 or 1");
   std::string err = analyze(nb, rowptr, colind, h->an, true, h->opt.coloring);
@@ -1151,9 +1154,11 @@ int gbilu_factor(void *handle, const double *vals) {
   if (!vals) return h->fail(GBILU_BAD_INPUT, "vals must not be NULL");
   auto t0 = std::chrono::steady_clock::now();
   h->factored = false;
+  h->fpga.reset();
   const Analysis &an = h->an;
   if (h->opt.factor_on_device && h->opt.device >= 0) {
     CK(cudaSetDevice(h->opt.device));
+    h->pvals.clear();   // the host copies are only made when asked for
     const int rc = factor_device(h, vals);
     if (rc) return rc;
     h->factored = true;
@@ -1202,6 +1207,55 @@ int gbilu_get_factors(void *handle, double *lu, double *dinv) {
   }
   if (lu) memcpy(lu, h->lu.data(), h->lu.size() * sizeof(double));
   if (dinv) memcpy(dinv, h->dinv.data(), h->dinv.size() * sizeof(double));
+  return GBILU_OK;
+}
+
+int gbilu_fpga_export(void *handle, const double *b, const double *x0, int *vector_sizes,
+                      int *nnz_sizes, void *const *vp) {
+  Handle *h = static_cast<Handle *>(handle);
+  if (!h) return GBILU_BAD_INPUT;
+  if (!h->factored) return h->fail(GBILU_NOT_READY, "gbilu_factor has not been called");
+  int rc = gbilu_get_factors(h, nullptr, nullptr);   // host copies of the factors
+  if (rc) return rc;
+  const Analysis &an = h->an;
+  if (h->pvals.size() != (size_t)an.nnzb * 9) {
+    // factored on the device: the permuted A from the uploaded input values
+    std::vector<double> in((size_t)an.nnzb * 9);
+    CK(cudaSetDevice(h->opt.device));
+    CK(cudaMemcpy(in.data(), h->vals_in.p, in.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    h->pvals.resize(in.size());
+    permute_values(an, in.data(), h->pvals.data());
+  }
+  if (!vp || !h->fpga) {
+    auto ex = std::make_unique<FpgaExport>();
+    const std::string err = fpga_export(an, h->pvals.data(), h->lu.data(), h->dinv.data(), *ex);
+    if (!err.empty()) return h->fail(GBILU_BAD_INPUT, "gbilu_fpga_export: %s", err.c_str());
+    h->fpga = std::move(ex);
+  }
+  const FpgaExport &ex = *h->fpga;
+  if (vector_sizes) memcpy(vector_sizes, ex.vector_sizes, sizeof ex.vector_sizes);
+  if (nnz_sizes) memcpy(nnz_sizes, ex.nnz_sizes, sizeof ex.nnz_sizes);
+  if (!vp) return GBILU_OK;
+  for (int m = 0; m < 3; ++m) {
+    void *const *v = vp + 6 * m;
+    if (!v[0] || !v[1] || !v[2] || !*(double *const *)v[2] || !v[3] || !v[4])
+      return h->fail(GBILU_BAD_INPUT, "gbilu_fpga_export: a vector pointer is NULL");
+    memcpy(v[0], ex.sizes[m].data(), ex.sizes[m].size() * sizeof(unsigned int));
+    memcpy(v[1], ex.pidx[m].data(), ex.pidx[m].size() * sizeof(unsigned int));
+    memcpy(*(double *const *)v[2], ex.vals[m].data(), ex.vals[m].size() * sizeof(double));
+    memcpy(v[3], ex.cols[m].data(), ex.cols[m].size() * sizeof(unsigned short));
+    memcpy(v[4], ex.nrs[m].data(), ex.nrs[m].size());
+  }
+  if (!vp[18] || !vp[19] || !vp[20])
+    return h->fail(GBILU_BAD_INPUT, "gbilu_fpga_export: a vector pointer is NULL");
+  memcpy(vp[18], ex.blkdiag.data(), ex.blkdiag.size() * sizeof(double));
+  // rhs and x0 in the permuted numbering of the exported rows
+  double *rhs = static_cast<double *>(vp[19]), *xx = static_cast<double *>(vp[20]);
+  for (int i = 0; i < an.nb; ++i)
+    for (int r = 0; r < 3; ++r) {
+      rhs[3 * i + r] = b ? b[3 * (size_t)an.perm[i] + r] : 0.0;
+      xx[3 * i + r] = x0 ? x0[3 * (size_t)an.perm[i] + r] : 0.0;
+    }
   return GBILU_OK;
 }
 

@@ -111,6 +111,7 @@ def load():
                                        C.POINTER(Result)]
     L.gbilu_dot_check.argtypes = [VP, C.c_int, VP, VP, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)]
+    L.gbilu_fpga_export.argtypes = [VP, VP, VP, VP, VP, VP]
     L.gbilu_get_stats.argtypes = [VP, C.POINTER(Stats)]
     L.gbilu_bench_kernel.argtypes = [VP, C.c_int, C.c_int, C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), C.POINTER(C.c_int)]
@@ -293,6 +294,51 @@ class GbIlu:
         self._check(self.L.gbilu_dot_check(self.h, x.size, x.ctypes.data, y.ctypes.data,
                                            C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def fpga_export(self, b=None, x0=None):
+        """The system as the Alveo kernel's input arrays (gbilu_fpga_export):
+        a dict with vector_sizes[18], nnz_sizes[3] and per matrix A, L, U
+        the color sizes (8-word header + 4 per part), P indices, values,
+        column indices, new-row offsets; the block diagonal, rhs and x0
+        (permuted); and 'pointers', the 21 vectorPointers (kept alive with
+        the arrays)."""
+        vs = np.zeros(18, np.int32)
+        nz = np.zeros(3, np.int32)
+        self._check(self.L.gbilu_fpga_export(self.h, None, None, vs.ctypes.data, nz.ctypes.data,
+                                             None))
+        out = {"vector_sizes": vs, "nnz_sizes": nz}
+        vp = (C.c_void_p * 21)()
+        keep = []
+        for m, name in enumerate("ALU"):
+            base = 6 * m
+            arrs = {"sizes": np.zeros(8 + 4 * int(vs[base + 2]), np.uint32),
+                    "pidx": np.zeros(int(vs[base + 3]), np.uint32),
+                    "vals": np.zeros(int(nz[m]), np.float64),
+                    "cols": np.zeros(int(vs[base + 1]), np.uint16),
+                    "nrs": np.zeros(int(vs[base + 4]), np.uint8)}
+            vptr = (C.c_void_p * 1)(arrs["vals"].ctypes.data)
+            keep.append(vptr)
+            vp[base + 0] = arrs["sizes"].ctypes.data
+            vp[base + 1] = arrs["pidx"].ctypes.data
+            vp[base + 2] = C.cast(vptr, C.c_void_p).value
+            vp[base + 3] = arrs["cols"].ctypes.data
+            vp[base + 4] = arrs["nrs"].ctypes.data
+            out[name] = arrs
+        n = int(vs[0])
+        out["blkdiag"] = np.zeros(int(vs[5]), np.float64)
+        out["rhs"] = np.zeros(n)
+        out["x0"] = np.zeros(n)
+        vp[18] = out["blkdiag"].ctypes.data
+        vp[19] = out["rhs"].ctypes.data
+        vp[20] = out["x0"].ctypes.data
+        bb = None if b is None else _f64(b)
+        xx = None if x0 is None else _f64(x0)
+        self._check(self.L.gbilu_fpga_export(self.h, None if bb is None else bb.ctypes.data,
+                                             None if xx is None else xx.ctypes.data,
+                                             vs.ctypes.data, nz.ctypes.data, vp))
+        out["pointers"] = vp
+        out["_keep"] = keep
+        return out
 
     def stats(self):
         s = Stats()

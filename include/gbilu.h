@@ -341,6 +341,26 @@ int gbilu_fpga_pack(unsigned int config_bits, const int *processed_sizes,
                     const int *vector_sizes, int fill_results,
                     unsigned char *const *banks);
 
+/* Exports the analyzed and factored system as the backend's vectorPointers
+ * that fpga_copy_host_datamem packs for the Alveo kernel
+ * (fpga_functions_bicgstab.cpp:528-545 sizes, :606-629 arrays): scalar rows
+ * in the color-permuted order, every color cut into parts ("colors" of the
+ * kernel) within the kernel's limits (2048 rows, 8192 vector-copy entries
+ * and 32768 values a part, 256 parts, 163840 unknowns, 2^21 values:
+ * alveo_u280/rtl/pkg/constants.vhd:76-105; larger systems ->
+ * GBILU_BAD_INPUT naming the limit). With vp == NULL it fills
+ * vector_sizes[18] (rows, values, colors, vector-copy entries, new-row
+ * offsets, block diagonal; for A, L, U) and nnz_sizes[3]; then the caller
+ * allocates vp[0,6,12] color sizes (8 + 4*colors words), vp[1,7,13] P
+ * indices (uint32), vp[2,8,14] a double* to the values, vp[3,9,15] column
+ * indices (uint16), vp[4,10,16] new-row offsets (uint8), vp[18] the block
+ * diagonal, vp[19] rhs and vp[20] x0 (3*nb doubles, permuted; b and x0 may
+ * be NULL for zeros) and calls again with vp. The same arrays then go to
+ * gbilu_fpga_pack. The format follows the kernel's RTL; gbilu_fpga_export.cpp
+ * states it and the RTL lines it rests on. */
+int gbilu_fpga_export(void *handle, const double *b, const double *x0, int *vector_sizes,
+                      int *nnz_sizes, void *const *vector_pointers);
+
 /* Writes a solve's outcome as the kernel's debug buffer (lines x 8 words):
  * line 0 = general status (signature, aborted / no-results flags, run length
  * in ns), line 1 = final status line (half-iteration counter, four-norm ring),
