@@ -1663,15 +1663,26 @@ int gbilu_bench_kernel(void *handle, int which, int reps, double *avg_ms, double
   CK(cudaMemcpyAsync(h->v64.p.p, x.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   if (h->with_32) k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0, h->v64.p.p, h->v32.p.p);
   if (which >= 4) {
-    // every work vector of the iteration holds the same data, so that the
-    // dots are nonzero and no kernel stops the run
+    // every work vector of the iteration holds its own pseudo-random data,
+    // so that the dots and norms are nonzero and no kernel stops the run
     Vecs<double> &w = h->v64;
-    for (DevBuf<double> *b : {&w.x, &w.r, &w.rt, &w.ph, &w.v, &w.s, &w.sh, &w.t, &w.y})
-      CK(cudaMemcpyAsync(b->p, w.p.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    std::vector<double> xv(n);
+    int k = 0;
+    for (DevBuf<double> *b : {&w.x, &w.r, &w.rt, &w.ph, &w.v, &w.s, &w.sh, &w.t, &w.y}) {
+      ++k;
+      for (int i = 0; i < n; ++i) {
+        z ^= z << 13; z ^= z >> 7; z ^= z << 17;
+        xv[i] = ((double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5) * k;
+      }
+      CK(cudaMemcpyAsync(b->p, xv.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+      CK(cudaStreamSynchronize(h->st));
+    }
     if (h->with_32) {
       Vecs<float> &f = h->v32;
-      for (DevBuf<float> *b : {&f.x, &f.r, &f.rt, &f.ph, &f.v, &f.s, &f.sh, &f.t, &f.y})
-        CK(cudaMemcpyAsync(b->p, f.p.p, n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+      DevBuf<double> *src[9] = {&w.x, &w.r, &w.rt, &w.ph, &w.v, &w.s, &w.sh, &w.t, &w.y};
+      DevBuf<float> *dst[9] = {&f.x, &f.r, &f.rt, &f.ph, &f.v, &f.s, &f.sh, &f.t, &f.y};
+      for (int j = 0; j < 9; ++j)
+        k_scale_convert<<<g, kThreads, 0, h->st>>>(n, 1.0, src[j]->p, dst[j]->p);
     }
   }
   // the iteration's other kernels (4-8 FP64, 9-13 FP32): the SpMV with the
