@@ -362,21 +362,25 @@ def iteration_budget(g, g64, st, b_dev, x_dev, local):
 def analysis_timing(s, local):
     """Analysis (coloring, ordering, device layout and upload) and ILU0
     factorization of the headline system, timed separately: host-only
-    analysis, analysis of a device handle, host factorization (with the
-    upload), device factorization."""
+    analysis; the analysis of a device handle with the coloring on the host
+    and on the GPU (the coloring's own time beside it); host factorization
+    (with the upload) and device factorization."""
     from fpga_gb300 import GbIlu
     out = {}
     with GbIlu(device=-1) as h:
         h.analyze(s.rowptr, s.colind)
         out["analyze_ms_host_only"] = h.stats()["analyze_ms"]
     for dev in (False, True):
-        with GbIlu(device=local, factor_on_device=dev) as h:
+        with GbIlu(device=local, factor_on_device=dev, color_on_device=dev) as h:
             h.analyze(s.rowptr, s.colind)
+            h.analyze(s.rowptr, s.colind)   # the second analysis (warm)
             h.factor(s.vals)
-            h.factor(s.vals)          # the second factorization (warm)
+            h.factor(s.vals)                # the second factorization (warm)
             st = h.stats()
-            out["analyze_ms_device_handle"] = st["analyze_ms"]
-            out["factor_ms_device" if dev else "factor_ms_host"] = st["factor_ms"]
+            key = "device" if dev else "host"
+            out["analyze_ms_" + key + "_coloring"] = st["analyze_ms"]
+            out["color_ms_" + key] = st["color_ms"]
+            out["factor_ms_" + key] = st["factor_ms"]
     return out
 
 

@@ -20,7 +20,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(LIBDIR, "libgbilu.so")
 SOURCES = ["gbilu_host.cpp", "gbilu_api.cu", "gbilu_noalloc.cu", "gbilu_fpga_compat.cpp",
-           "gbilu_fpga_export.cpp"]
+           "gbilu_fpga_export.cpp", "gbilu_color.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

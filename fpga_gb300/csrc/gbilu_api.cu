@@ -78,7 +78,7 @@ struct Handle {
   Analysis an;
   bool analyzed = false, factored = false;
   std::vector<double> pvals, lu, dinv;   // host: permuted A, factors
-  double analyze_ms = 0, factor_ms = 0;
+  double analyze_ms = 0, factor_ms = 0, color_ms = 0;
   // device
   bool dev_ready = false;
   int sm_count = 0;
@@ -1077,6 +1077,7 @@ int gbilu_default_options(gbilu_options *o) {
   o->stage_small_steps = 1;
   o->coloring = 0;
   o->stream_large_steps = 0;
+  o->color_on_device = 0;
   return GBILU_OK;
 }
 
@@ -1122,7 +1123,21 @@ int gbilu_analyze(void *handle, int nb, const int *rowptr, const int *colind) {
   h->fpga.reset();
   if (h->opt.coloring != 0 && h->opt.coloring != 1)
     return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: coloring must be 0 or 1");
-  std::string err = analyze(nb, rowptr, colind, h->an, true, h->opt.coloring);
+  std::vector<int> dcolors;
+  h->color_ms = 0.0;
+  if (h->opt.color_on_device && h->opt.device >= 0 && h->opt.coloring == 0) {
+    // the pattern is checked first: the device coloring assumes it is valid
+    std::string perr = check_pattern(nb, rowptr, colind);
+    if (!perr.empty()) return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: %s", perr.c_str());
+    dcolors.resize(nb);
+    int nc = 0;
+    perr = color_parity_device(nb, rowptr, colind, h->opt.device, dcolors.data(), &nc, &h->color_ms);
+    if (!perr.empty())
+      return h->fail(GBILU_CUDA_ERROR, "gbilu_analyze: device coloring: %s", perr.c_str());
+  }
+  std::string err = analyze(nb, rowptr, colind, h->an, true, h->opt.coloring,
+                            dcolors.empty() ? nullptr : dcolors.data(),
+                            dcolors.empty() ? &h->color_ms : nullptr);
   if (!err.empty()) return h->fail(GBILU_BAD_INPUT, "gbilu_analyze: %s", err.c_str());
   h->analyzed = true;
   if (h->opt.device >= 0) {
@@ -1503,6 +1518,8 @@ int gbilu_get_stats(void *handle, gbilu_stats *s) {
   s->last_launches = h->last_launches;
   s->factor_ms = h->factor_ms;
   s->analyze_ms = h->analyze_ms;
+  s->color_ms = h->color_ms;
+  s->color_on_device = h->opt.color_on_device && h->opt.device >= 0 && h->opt.coloring == 0;
   for (int p = 0; p < 2; ++p) {
     s->ring_stages[p] = h->stage[p][0].ring_ns;
     s->ring_stage_bytes[p] = h->stage[p][0].ring_stride;

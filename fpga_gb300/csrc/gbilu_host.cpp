@@ -2,6 +2,7 @@
 #include "gbilu_host.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -211,7 +212,7 @@ Csr transpose_csr(int nb, const Csr &m) {
 }  // namespace
 
 std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
-                    bool with_transposes, int coloring) {
+                    bool with_transposes, int coloring, const int *colors, double *color_ms) {
   std::string err = check_pattern(nb, rowptr, colind);
   if (!err.empty()) return err;
   an = Analysis();
@@ -220,8 +221,17 @@ std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
   an.rowptr.assign(rowptr, rowptr + nb + 1);
   an.colind.assign(colind, colind + an.nnzb);
   an.color.resize(nb);
-  an.ncolors = coloring == 1 ? color_greedy(nb, rowptr, colind, an.color.data())
-                             : color_parity_greedy(nb, rowptr, colind, an.color.data());
+  if (colors) {
+    std::copy(colors, colors + nb, an.color.begin());
+    an.ncolors = 1 + *std::max_element(colors, colors + nb);
+  } else {
+    const auto t0 = std::chrono::steady_clock::now();
+    an.ncolors = coloring == 1 ? color_greedy(nb, rowptr, colind, an.color.data())
+                               : color_parity_greedy(nb, rowptr, colind, an.color.data());
+    if (color_ms)
+      *color_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                      .count();
+  }
   const int C = an.ncolors;
 
   // Color-ordered permutation (counting sort). Inside a color, the rows that

@@ -80,9 +80,17 @@ int color_parity_greedy(int nb, const int *rowptr, const int *colind, int *color
 std::string check_pattern(int nb, const int *rowptr, const int *colind);
 
 // Builds everything above from an input pattern. Returns "" or an error.
-// coloring: 0 color_parity_greedy (default), 1 color_greedy.
+// coloring: 0 color_parity_greedy (default), 1 color_greedy; colors: a
+// coloring computed elsewhere (color_parity_device), or null. *color_ms gets
+// the time of the host coloring when it ran.
 std::string analyze(int nb, const int *rowptr, const int *colind, Analysis &an,
-                    bool with_transposes, int coloring = 0);
+                    bool with_transposes, int coloring = 0, const int *colors = nullptr,
+                    double *color_ms = nullptr);
+
+// color_parity_greedy on the GPU (gbilu_color.cu): the same colors; *ms
+// gets its device time (uploads, kernels, download).
+std::string color_parity_device(int nb, const int *rowptr, const int *colind, int device,
+                                int *color, int *ncolors, double *ms);
 
 // Block ILU(0) (IKJ) of the permuted matrix. pvals (nnzb*9, permuted order)
 // is overwritten with L (col < row) and U (col >= row); dinv[nb*9] gets the

@@ -28,7 +28,8 @@ class Options(C.Structure):
                 ("max_outer", C.c_int), ("verbose", C.c_int), ("sweep_mode", C.c_int),
                 ("factor_on_device", C.c_int), ("mixed_scheme", C.c_int),
                 ("ru_delta", C.c_double), ("stage_small_steps", C.c_int),
-                ("coloring", C.c_int), ("stream_large_steps", C.c_int)]
+                ("coloring", C.c_int), ("stream_large_steps", C.c_int),
+                ("color_on_device", C.c_int)]
 
 
 class Result(C.Structure):
@@ -54,7 +55,8 @@ class Stats(C.Structure):
                 ("factor_ms", C.c_double), ("analyze_ms", C.c_double),
                 ("alg_bytes_spmv", C.c_double * 2), ("alg_bytes_ilu", C.c_double * 2),
                 ("alg_bytes_iter", C.c_double * 2), ("ring_stages", C.c_int * 2),
-                ("ring_stage_bytes", C.c_int * 2), ("apply_smem_bytes", C.c_int * 2)]
+                ("ring_stage_bytes", C.c_int * 2), ("apply_smem_bytes", C.c_int * 2),
+                ("color_ms", C.c_double), ("color_on_device", C.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -140,7 +142,7 @@ class GbIlu:
                  timeout_ms=0.0, inner_tol=1e-1, inner_maxit=500, max_outer=30,
                  verbose=0, sweep_mode=1, factor_on_device=False, mixed_scheme=0,
                  ru_delta=0.1, stage_small_steps=True, coloring="parity",
-                 stream_large_steps=False):
+                 stream_large_steps=False, color_on_device=False):
         self.L = load()
         o = Options()
         self.L.gbilu_default_options(C.byref(o))
@@ -160,6 +162,7 @@ class GbIlu:
         o.stage_small_steps = int(stage_small_steps)
         o.coloring = {"parity": 0, "natural": 1}[coloring]
         o.stream_large_steps = int(stream_large_steps)
+        o.color_on_device = int(color_on_device)
         self.h = VP()
         rc = self.L.gbilu_create(C.byref(o), C.byref(self.h))
         if rc:

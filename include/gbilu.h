@@ -107,6 +107,9 @@ typedef struct {
                          across barriers) and the others compute from it;
                          0 (default): every warp loads its own rows (same
                          results) */
+  int color_on_device; /* 1: gbilu_analyze computes the parity-order coloring
+                         (coloring = 0) on the GPU, the same colors bit for
+                         bit; 0 (default): on the host */
 } gbilu_options;
 
 typedef struct {
@@ -157,6 +160,8 @@ typedef struct {
   int ring_stages[2];
   int ring_stage_bytes[2];
   int apply_smem_bytes[2];
+  double color_ms;          /* the coloring inside the last gbilu_analyze */
+  int color_on_device;      /* 1: it ran on the GPU */
 } gbilu_stats;
 
 /* fill *opt with defaults: FP64, relative tolerance, device 0, graph on,
