@@ -251,7 +251,7 @@ def gpu_bench(args, world, rank, local):
         ms, by, la = g.bench_kernel(name, reps=20)
         kern[name] = {"ms": ms, "alg_bytes": by, "launches": la, "gbs": by / ms / 1e6}
     trace = {"fp64": g.ilu_trace(fp32=False), "fp32": g.ilu_trace(fp32=True)}
-    budget = iteration_budget(g, g64, st, b_dev, x_dev, local)
+    budget = iteration_budget(g, g64, st, b_dev, x_dev, local) if not args.quick else None
     it_ms = value / max(1, (r0.half_iters + 1) / 2.0)
     solve_gbs = st["alg_bytes_iter"][0] / it_ms / 1e6 if it_ms > 0 else None
     traffic = None
@@ -297,7 +297,7 @@ def gpu_bench(args, world, rank, local):
                "kernels": kern,
                "ilu_phases_rows_us": trace,
                "iteration_budget": budget,
-               "analysis": analysis_timing(s, local),
+               "analysis": analysis_timing(s, local) if not args.quick else None,
                "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": 2 * n * 8,
                        "d2h_bytes_per_step": n * 8},
                "gpu_launches": int(launches),
