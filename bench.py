@@ -389,6 +389,7 @@ def cpu_baseline(s, tol, maxit):
     headline system at its tolerance (the line's cpu_baseline) and, under
     ``others``, the other workloads and tolerances the GPU numbers are
     quoted on (median of 3 solves each, after one warm-up)."""
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle_lib import Prepared
     from fpga_gb300.synth import make_config, CONFIGS
@@ -426,6 +427,23 @@ def cpu_baseline(s, tol, maxit):
         ms, r = timed(P2, s2.b, t, CONFIGS[wl]["maxit"], 3)
         others.append({"workload": wl, "form": "fp64 forward", "tol": t, "ms": ms,
                        "half_iters": r.half_iters})
+        if wl.startswith("c4"):
+            # the adjoint's transposed solve, g = W^T (W x - d)
+            from fpga_gb300.synth import adjoint_selection
+            x, _ = P2.solve_omp(s2.b, tol=t, maxit=CONFIGS[wl]["maxit"], nthreads=cores)
+            cells, d = adjoint_selection(s2.nb)
+            idx = (3 * cells[:, None] + np.arange(3)).reshape(-1)
+            gv = np.zeros(s2.n)
+            gv[idx] = x[idx] - d
+            P2.solve_omp(gv, tol=t, maxit=CONFIGS[wl]["maxit"], nthreads=cores, transpose=True)
+            tt = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                _, ra = P2.solve_omp(gv, tol=t, maxit=CONFIGS[wl]["maxit"], nthreads=cores,
+                                     transpose=True)
+                tt.append((time.perf_counter() - t0) * 1e3)
+            others.append({"workload": wl, "form": "fp64 adjoint (transposed solve)", "tol": t,
+                           "ms": statistics.median(tt), "half_iters": ra.half_iters})
     out["others"] = others
     return out
 

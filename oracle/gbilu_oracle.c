@@ -530,6 +530,59 @@ static void ilu_omp(int ncolors, const int *color_ptr, const int *rowptr,
   }
 }
 
+/* z = (LU)^-T p with the explicit transpose T of the factored matrix
+ * (blocks transposed): T's strictly lower blocks are U^T, its strictly
+ * upper ones L^T. Forward over colors with the transposed inverse diagonal
+ * blocks (U^T y = p), then backward with the unit diagonal (L^T z = y);
+ * the rows of one color are independent (structurally symmetric pattern). */
+static void ilu_t_omp(int ncolors, const int *color_ptr, const int *trowptr,
+                      const int *tcolind, const double *tlu, const double *dinv,
+                      const double *p, double *z) {
+  for (int c = 0; c < ncolors; ++c) {
+#pragma omp parallel for schedule(static)
+    for (int i = color_ptr[c]; i < color_ptr[c + 1]; ++i) {
+      double a[3] = {p[3 * i], p[3 * i + 1], p[3 * i + 2]};
+      for (int k = trowptr[i]; k < trowptr[i + 1] && tcolind[k] < i; ++k) {
+        const double *b = tlu + (size_t)k * 9, *yj = z + 3 * (size_t)tcolind[k];
+        for (int r = 0; r < 3; ++r)
+          a[r] -= b[r * 3] * yj[0] + b[r * 3 + 1] * yj[1] + b[r * 3 + 2] * yj[2];
+      }
+      const double *d = dinv + (size_t)i * 9;   /* (D^-1)^T: column r of d */
+      for (int r = 0; r < 3; ++r)
+        z[3 * i + r] = d[r] * a[0] + d[3 + r] * a[1] + d[6 + r] * a[2];
+    }
+  }
+  for (int c = ncolors - 1; c >= 0; --c) {
+#pragma omp parallel for schedule(static)
+    for (int i = color_ptr[c]; i < color_ptr[c + 1]; ++i) {
+      double a[3] = {z[3 * i], z[3 * i + 1], z[3 * i + 2]};
+      for (int k = trowptr[i + 1] - 1; k >= trowptr[i] && tcolind[k] > i; --k) {
+        const double *b = tlu + (size_t)k * 9, *zj = z + 3 * (size_t)tcolind[k];
+        for (int r = 0; r < 3; ++r)
+          a[r] -= b[r * 3] * zj[0] + b[r * 3 + 1] * zj[1] + b[r * 3 + 2] * zj[2];
+      }
+      z[3 * i] = a[0]; z[3 * i + 1] = a[1]; z[3 * i + 2] = a[2];
+    }
+  }
+}
+
+void orc_transpose_bsr(int nb, const int *rowptr, const int *colind, const double *vals,
+                       int *trowptr, int *tcolind, double *tvals) {
+  int *fill = (int *)calloc((size_t)nb + 1, sizeof(int));
+  for (int i = 0; i <= nb; ++i) trowptr[i] = 0;
+  for (int k = 0; k < rowptr[nb]; ++k) trowptr[colind[k] + 1]++;
+  for (int i = 0; i < nb; ++i) trowptr[i + 1] += trowptr[i];
+  for (int i = 0; i < nb; ++i) fill[i] = trowptr[i];
+  for (int i = 0; i < nb; ++i)             /* rows ascending: columns sorted */
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int p = fill[colind[k]]++;
+      tcolind[p] = i;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) tvals[(size_t)p * 9 + r * 3 + c] = vals[(size_t)k * 9 + c * 3 + r];
+    }
+  free(fill);
+}
+
 static double dot_omp(size_t n, const double *a, const double *b) {
   double s = 0;
 #pragma omp parallel for reduction(+ : s) schedule(static)
@@ -537,11 +590,35 @@ static double dot_omp(size_t n, const double *a, const double *b) {
   return s;
 }
 
+static int bicgstab_omp_core(int nb, int ncolors, const int *color_ptr,
+                             const int *rowptr, const int *colind, const double *avals,
+                             const double *lu, const double *dinv, const double *b,
+                             double *x, double tol, int absolute, int maxit,
+                             int nthreads, orc_result *res, int transpose);
+
 int orc_bicgstab_omp(int nb, int ncolors, const int *color_ptr,
                      const int *rowptr, const int *colind, const double *avals,
                      const double *lu, const double *dinv, const double *b,
                      double *x, double tol, int absolute, int maxit,
                      int nthreads, orc_result *res) {
+  return bicgstab_omp_core(nb, ncolors, color_ptr, rowptr, colind, avals, lu, dinv, b, x, tol,
+                           absolute, maxit, nthreads, res, 0);
+}
+
+int orc_bicgstab_omp_t(int nb, int ncolors, const int *color_ptr,
+                       const int *trowptr, const int *tcolind, const double *tavals,
+                       const double *tlu, const double *dinv, const double *b,
+                       double *x, double tol, int absolute, int maxit,
+                       int nthreads, orc_result *res) {
+  return bicgstab_omp_core(nb, ncolors, color_ptr, trowptr, tcolind, tavals, tlu, dinv, b, x,
+                           tol, absolute, maxit, nthreads, res, 1);
+}
+
+static int bicgstab_omp_core(int nb, int ncolors, const int *color_ptr,
+                             const int *rowptr, const int *colind, const double *avals,
+                             const double *lu, const double *dinv, const double *b,
+                             double *x, double tol, int absolute, int maxit,
+                             int nthreads, orc_result *res, int transpose) {
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -566,7 +643,7 @@ int orc_bicgstab_omp(int nb, int ncolors, const int *color_ptr,
   if (!absolute) bound = tol * norm0;
   for (int k = 0;; ++k) {
     half = 2 * k;
-    ilu_omp(ncolors, color_ptr, rowptr, colind, lu, dinv, p, ph);
+    (transpose ? ilu_t_omp : ilu_omp)(ncolors, color_ptr, rowptr, colind, lu, dinv, p, ph);
     spmv_omp(nb, rowptr, colind, avals, ph, v);
     double vr = dot_omp(n, v, rt), alpha = rho / vr;
     if (vr == 0.0 || !isfinite(alpha)) { status = ORC_BREAKDOWN; break; }
@@ -578,7 +655,7 @@ int orc_bicgstab_omp(int nb, int ncolors, const int *color_ptr,
     if (!(ns > bound)) { status = ORC_OK; break; }
     if (k == maxit) { status = ORC_MAXIT; break; }
     half = 2 * k + 1;
-    ilu_omp(ncolors, color_ptr, rowptr, colind, lu, dinv, s, ph);
+    (transpose ? ilu_t_omp : ilu_omp)(ncolors, color_ptr, rowptr, colind, lu, dinv, s, ph);
     spmv_omp(nb, rowptr, colind, avals, ph, t);
     double ts = dot_omp(n, t, s), tt = dot_omp(n, t, t), omega = ts / tt;
     if (tt == 0.0 || !isfinite(omega)) { status = ORC_BREAKDOWN; break; }

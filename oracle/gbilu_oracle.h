@@ -81,6 +81,12 @@ int orc_inv3(const double *a, double *out);
 int orc_bilu0(int nb, const int *rowptr, const int *colind, double *vals,
               double *dinv);
 
+/* Explicit transpose of a BSR matrix with sorted columns: the pattern
+ * transposed, each 3x3 block transposed; trowptr[nb+1], tcolind and
+ * tvals[9*nnzb] sized like the input. */
+void orc_transpose_bsr(int nb, const int *rowptr, const int *colind, const double *vals,
+                       int *trowptr, int *tcolind, double *tvals);
+
 /* y = A x */
 void orc_spmv(int nb, const int *rowptr, const int *colind, const double *vals,
               const double *x, double *y);
@@ -134,6 +140,16 @@ int orc_bicgstab_omp(int nb, int ncolors, const int *color_ptr,
                      const double *lu, const double *dinv, const double *b,
                      double *x, double tol, int absolute, int maxit,
                      int nthreads, orc_result *res);
+
+/* The same for the transposed system A^T x = b (the adjoint), on the
+ * explicit transposes of A and of the factored matrix (orc_transpose_bsr):
+ * the preconditioner is (LU)^-T, U^T with the transposed inverse diagonal
+ * blocks forward over the colors, then L^T backward. */
+int orc_bicgstab_omp_t(int nb, int ncolors, const int *color_ptr,
+                       const int *trowptr, const int *tcolind, const double *tavals,
+                       const double *tlu, const double *dinv, const double *b,
+                       double *x, double tol, int absolute, int maxit,
+                       int nthreads, orc_result *res);
 
 /* Mixed-precision restatement: A, L, U and dinv rounded to float, inner
  * BiCGSTAB on float vectors with double dot accumulation, outer iterative

@@ -61,6 +61,9 @@ def lib():
                                        C.c_int, C.c_int, C.c_int,
                                        C.POINTER(OrcResult)]
         L.orc_bicgstab_omp.restype = C.c_int
+        L.orc_bicgstab_omp_t.argtypes = L.orc_bicgstab_omp.argtypes
+        L.orc_bicgstab_omp_t.restype = C.c_int
+        L.orc_transpose_bsr.argtypes = [C.c_int, I32P, I32P, F64P, I32P, I32P, F64P]
         L.orc_mixed_ir.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P,
                                    F64P, C.c_double, C.c_double, C.c_int, C.c_int,
                                    C.POINTER(OrcResult), C.POINTER(C.c_int),
@@ -138,13 +141,32 @@ class Prepared:
             return out, res, hist[:min(res.nhist, hist_cap)]
         return out, res
 
-    def solve_omp(self, b, tol=1e-2, maxit=200, nthreads=0):
+    def transposes(self):
+        """Explicit transposes of A and of the factored matrix (cached)."""
+        if not hasattr(self, "_t"):
+            nnz = self.colind.size
+            t = []
+            for v in (self.avals, self.lu):
+                rp, ci, tv = np.empty(self.nb + 1, np.int32), np.empty(nnz, np.int32), \
+                    np.empty(nnz * 9)
+                lib().orc_transpose_bsr(self.nb, self.rowptr, self.colind, v, rp, ci, tv)
+                t.append((rp, ci, tv))
+            self._t = t
+        return self._t
+
+    def solve_omp(self, b, tol=1e-2, maxit=200, nthreads=0, transpose=False):
         x = np.zeros(3 * self.nb)
         res = OrcResult()
-        lib().orc_bicgstab_omp(self.nb, self.ncolors, self.color_ptr, self.rowptr,
-                               self.colind, self.avals, self.lu, self.dinv,
-                               self.to_perm(b), x, tol, 0, maxit, nthreads,
-                               C.byref(res))
+        if transpose:
+            (rp, ci, ta), (_, _, tlu) = self.transposes()
+            lib().orc_bicgstab_omp_t(self.nb, self.ncolors, self.color_ptr, rp, ci, ta, tlu,
+                                     self.dinv, self.to_perm(b), x, tol, 0, maxit, nthreads,
+                                     C.byref(res))
+        else:
+            lib().orc_bicgstab_omp(self.nb, self.ncolors, self.color_ptr, self.rowptr,
+                                   self.colind, self.avals, self.lu, self.dinv,
+                                   self.to_perm(b), x, tol, 0, maxit, nthreads,
+                                   C.byref(res))
         return self.from_perm(x), res
 
     def mixed(self, b, tol=1e-8, inner_tol=1e-4, inner_maxit=500, max_outer=20):

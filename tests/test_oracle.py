@@ -212,3 +212,17 @@ def test_golden_fixtures(name):
     xs, r = P.solve(s.b, tol=float(f["tol"]), maxit=500)
     assert r.half_iters == int(f["half_iters"])
     assert np.array_equal(xs, f["x"])
+
+
+def test_threaded_transposed_solve_matches_sequential(prep):
+    """The OpenMP transposed solve (the adjoint's CPU baseline) against the
+    sequential transposed solve: same half-iterations, same solution."""
+    P = prep
+    s = P.sys
+    g = np.random.default_rng(4).standard_normal(s.n)
+    x1, r1 = P.solve(g, tol=1e-8, maxit=500, transpose=True)
+    x2, r2 = P.solve_omp(g, tol=1e-8, maxit=500, nthreads=4, transpose=True)
+    assert r1.status == r2.status == 0 and r1.half_iters == r2.half_iters
+    assert np.linalg.norm(x1 - x2) <= 1e-10 * np.linalg.norm(x1)
+    At = s.to_scipy().T
+    assert np.linalg.norm(At @ x2 - g) <= 1e-7 * np.linalg.norm(g)
