@@ -100,6 +100,7 @@ struct Handle {
   Vecs<double> v64;
   Vecs<float> v32;
   DevBuf<double> b64, io64, io64b, partials, dA;
+  DevBuf<int> x0nz;                        // set when x0 has a nonzero entry
   // device factorization: permuted values (factored in place), inverses
   DevBuf<int> pdiag, bad;
   DevBuf<double> pbuf, vals_in, dinvp;
@@ -478,13 +479,13 @@ void apply_prec(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *src, T *
 
 template <typename V, typename T, int MODE>
 void spmv(Handle *h, cudaStream_t s, const Ops<V, T> &o, const T *x, T *y, const T *w,
-          int &launches) {
+          int &launches, const int *x_nonzero = nullptr) {
   const int S = h->an.S;
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spmv<V, T, MODE>, kThreads, 0);
   const int grid = std::max(1, std::min((S + kWarps - 1) / kWarps, std::max(1, per_sm) * h->sm_count));
   k_spmv<V, T, MODE><<<grid, kThreads, 0, s>>>(
-      h->ctl.p, S, h->srows.p, o.offA, o.colA, o.valA, x, y, w, h->partials.p);
+      h->ctl.p, S, h->srows.p, o.offA, o.colA, o.valA, x, y, w, h->partials.p, x_nonzero);
   ++launches;
 }
 
@@ -695,6 +696,7 @@ void release_device(Handle *h) {
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
   h->io64.release(); h->io64b.release(); h->partials.release(); h->dA.release();
+  h->x0nz.release();
   h->ctl.release();
   h->device_bytes = 0;
 }
@@ -764,6 +766,8 @@ int setup_device(Handle *h) {
   CK(h->io64b.alloc(n));
   const size_t maxgrid = std::max<size_t>((size_t)h->sm_count * 8, (size_t)(an.S + kWarps - 1) / kWarps) + 1;
   CK(h->partials.alloc(2 * maxgrid));
+  CK(h->x0nz.alloc(1));
+  CK(cudaMemset(h->x0nz.p, 0xff, sizeof(int)));   // "nonzero" until a gather clears it
   CK(h->ctl.alloc(2));
   if (h->opt.factor_on_device) {
     CK(h->pdiag.alloc(an.nb));
@@ -870,7 +874,8 @@ int solve64(Handle *h, bool transpose, double tol, int maxit, Ctl &out, long lon
   const unsigned long long tmo = (unsigned long long)(h->opt.timeout_ms * 1e6);
   k_ctl_init<<<1, 32, 0, h->st>>>(h->ctl.p, tol, h->opt.absolute_tol, maxit, tmo);
   int l = 1;
-  spmv<double, double, SPMV_PLAIN>(h, h->st, o, w.x.p, w.r.p, nullptr, l);   // r = A x0
+  // r = A x0 (zeros without reading A when the gather of x0 found none)
+  spmv<double, double, SPMV_PLAIN>(h, h->st, o, w.x.p, w.r.p, nullptr, l, h->x0nz.p);
   launches += l;
   if (b_ready) CK(cudaStreamWaitEvent(h->st, b_ready, 0));
   k_init_resid<double><<<reduce_grid(h, n), kThreads, 0, h->st>>>(
@@ -1323,10 +1328,12 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
   const bool overlap_b = fp64 && !device_ptrs;
   if (!device_ptrs && !mapped_x)
     CK(cudaMemcpyAsync(h->io64b.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync(h->x0nz.p, 0, sizeof(int), h->st));
   if (mapped_x)   // host side read in order, device side written permuted
-    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, dx, h->v64.x.p);
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->iperm.p, dx, h->v64.x.p, h->x0nz.p);
   else
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0);
+    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, dx, h->v64.x.p, 1.0,
+                                                        h->x0nz.p);
   cudaStream_t sb = h->st;
   if (overlap_b) {
     CK(cudaEventRecord(h->e_x, h->st));

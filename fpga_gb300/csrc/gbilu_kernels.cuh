@@ -333,13 +333,23 @@ enum SpmvMode { SPMV_PLAIN = 0, SPMV_RESID = 1, SPMV_ALPHA = 2, SPMV_OMEGA = 3, 
 #ifndef GBILU_SPMV64_MINB
 #define GBILU_SPMV64_MINB 3
 #endif
+// x_nonzero (PLAIN only, may be null): a flag the producer of x set when
+// any entry of x is not zero; when it is clear y = A x = 0 is written
+// without reading A (the initial residual of a solve from x0 = 0).
 template <typename V, typename T, int MODE>
 __global__ void __launch_bounds__(kThreads, sizeof(V) == 4 ? GBILU_SPMV32_MINB : GBILU_SPMV64_MINB)
 k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ off,
        const int *__restrict__ col, const V *__restrict__ val, const T *__restrict__ x,
-       T *__restrict__ y, const T *__restrict__ w, double *partials) {
+       T *__restrict__ y, const T *__restrict__ w, double *partials,
+       const int *x_nonzero = nullptr) {
   if (MODE == SPMV_TRUE && (!ctl->ru || ctl->done)) return;
   if (MODE != SPMV_PLAIN && MODE != SPMV_RESID && ctl->done) return;
+  if (MODE == SPMV_PLAIN && x_nonzero && !*x_nonzero) {
+    const int n = 3 * (srows[S - 1].x + srows[S - 1].y);
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+      y[i] = (T)0;
+    return;
+  }
   constexpr bool RES = MODE == SPMV_RESID || MODE == SPMV_TRUE;
   // persistent grid: each warp walks slices warp, warp + all warps, ...;
   // one reduction per CTA at the end instead of one per 8 slices
@@ -1568,24 +1578,34 @@ k_finish_x(const Ctl *ctl, int n, T *__restrict__ x, const T *__restrict__ ph) {
 // permutation, precision conversion, refinement and gradient kernels
 // --------------------------------------------------------------------------
 
-// out[3i+r] = in[3 perm[i] + r]  (original -> permuted numbering)
+// out[3i+r] = in[3 perm[i] + r]  (original -> permuted numbering); nz (may
+// be null) is set when any value is not zero
 template <typename TI, typename TO>
 __global__ void k_gather(int nb, const int *__restrict__ perm, const TI *__restrict__ in,
-                         TO *__restrict__ out, double scale) {
+                         TO *__restrict__ out, double scale, int *nz = nullptr) {
+  bool any = false;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < 3 * nb; i += gridDim.x * kThreads) {
     const int b = i / 3, r = i - 3 * b;
-    out[i] = (TO)((double)in[3 * perm[b] + r] * scale);
+    const TI v = in[3 * perm[b] + r];
+    any |= v != (TI)0;
+    out[i] = (TO)((double)v * scale);
   }
+  if (nz && __syncthreads_or(any) && threadIdx.x == 0) *nz = 1;
 }
 
-// out[3 perm[i] + r] = in[3i+r]  (permuted -> original numbering)
+// out[3 perm[i] + r] = in[3i+r]  (permuted -> original numbering); nz as
+// for k_gather
 template <typename T>
 __global__ void k_scatter(int nb, const int *__restrict__ perm, const T *__restrict__ in,
-                          T *__restrict__ out) {
+                          T *__restrict__ out, int *nz = nullptr) {
+  bool any = false;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < 3 * nb; i += gridDim.x * kThreads) {
     const int b = i / 3, r = i - 3 * b;
-    out[3 * perm[b] + r] = in[i];
+    const T v = in[i];
+    any |= v != (T)0;
+    out[3 * perm[b] + r] = v;
   }
+  if (nz && __syncthreads_or(any) && threadIdx.x == 0) *nz = 1;
 }
 
 // out = (float)(scale * in): the FP32 right-hand side of a refinement step

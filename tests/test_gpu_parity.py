@@ -438,3 +438,20 @@ def test_ring_500k_bit_identical(built_lib, precision, coloring):
         P = Prepared(s, coloring=coloring)
         assert rel(runs[0][2], P.ilu_apply(p)) < KERNEL_TOL
         assert rel(runs[0][3], P.ilu_apply(p, True)) < KERNEL_TOL
+
+
+def test_zero_start_shortcut(case):
+    """From x0 = 0 the initial A x0 is not computed (the gather of x0 finds
+    no nonzero entry): -0.0 entries give the same bits as +0.0, and a single
+    nonzero entry still takes the full path, matching the oracle."""
+    s, P, g = case
+    x1, r1 = g.solve(s.b, x0=np.zeros(s.n), tol=1e-6, maxit=500)
+    x2, r2 = g.solve(s.b, x0=np.full(s.n, -0.0), tol=1e-6, maxit=500)
+    assert r1.half_iters == r2.half_iters and np.array_equal(x1, x2)
+    x0 = np.zeros(s.n)
+    x0[s.n // 2] = 1e-3
+    x_ref, r_ref = P.solve(s.b, x0=x0, tol=1e-6, maxit=500)
+    x3, r3 = g.solve(s.b, x0=x0, tol=1e-6, maxit=500)
+    assert r3.half_iters == r_ref.half_iters
+    assert rel(x3, x_ref) < SOLUTION_TOL
+    assert abs(r3.norm0 - r_ref.norm0) <= 1e-12 * r_ref.norm0
