@@ -46,6 +46,10 @@ int main(int argc, char **argv) {
   gbilu_default_options(&opt);
   opt.device = atoi(argv[3]);
   opt.precision = precision;
+  // as a simulator backend would run it: refactorization and coloring on
+  // the GPU (no effect on a host-only handle)
+  opt.factor_on_device = 1;
+  opt.color_on_device = 1;
   gbilu::BsrBridge bridge(tol, maxit, &opt);
   const bool dev = opt.device >= 0;
 
