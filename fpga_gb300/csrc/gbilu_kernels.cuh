@@ -56,6 +56,7 @@ struct Ctl {
   double true_norm;               // ||b - A x|| of the last replacement (FP64)
   int replacements;
   unsigned long long phase_ns[kMaxPhases + 1];   // traced ILU apply: phase starts
+  unsigned int step_next[kMaxPhases];   // single-launch apply: next slice of a large step
 };
 
 // --------------------------------------------------------------------------
@@ -63,6 +64,41 @@ struct Ctl {
 // --------------------------------------------------------------------------
 
 template <typename T> __device__ __forceinline__ T ldg_stream(const T *p) { return __ldcs(p); }
+
+// L2 prefetch of matrix slices ahead of the warp that will read them (the
+// large steps of the single-launch apply, the SpMV): rounds of the grid's
+// warps ahead; 0 turns it off.
+#ifndef GBILU_SPMV_PREFETCH
+#define GBILU_SPMV_PREFETCH 0
+#endif
+#ifndef GBILU_PREFETCH_EVICT_FIRST
+#define GBILU_PREFETCH_EVICT_FIRST 1
+#endif
+// The prefetched lines are marked evict-first, like the streaming loads
+// that read them: they must not push the solver's vectors out of L2.
+__device__ __forceinline__ void prefetch_l2(const void *p, unsigned int bytes) {
+  if (GBILU_PREFETCH_EVICT_FIRST) {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    asm volatile("cp.async.bulk.prefetch.L2.global.L2::cache_hint [%0], %1, %2;" ::"l"(p),
+                 "r"(bytes), "l"(pol)
+                 : "memory");
+  } else {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+  }
+}
+// The slice's blocks (values and column indices: contiguous, 16-byte
+// aligned ranges of the sliced layout) and, when the step reads it, its D
+// block; o = off[s], w = off[s + 1] - o.
+template <typename V>
+__device__ __forceinline__ void prefetch_slice(int s, int o, int w, const int *col, const V *val,
+                                               const V *dmat, bool d) {
+  if (w > 0) {
+    prefetch_l2(val + (size_t)o * 9 * 32, (unsigned int)w * 9 * 32 * (unsigned int)sizeof(V));
+    prefetch_l2(col + (size_t)o * 32, (unsigned int)w * 32 * (unsigned int)sizeof(int));
+  }
+  if (d) prefetch_l2(dmat + (size_t)s * 9 * 32, 9 * 32 * (unsigned int)sizeof(V));
+}
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -203,6 +239,7 @@ __global__ void k_ctl_init(Ctl *c, double tol, int absolute, int maxit,
     c->rho_prev = 0.0;
     c->true_norm = 0.0;
     c->replacements = 0;
+    for (int q = 0; q < kMaxPhases; ++q) c->step_next[q] = 0u;
   }
 }
 
@@ -362,11 +399,26 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
   // solve gains 1.5 %). FP64 is bound by the FP64 unit, and the extra
   // registers spill in its dot modes: it loads them per slice.
   constexpr bool AHEAD = sizeof(V) == 4;
+  // FP32 matrices only: the FP64 SpMV is bound by the FP64 unit
+  constexpr bool PF = sizeof(V) == 4;
   int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
   int2 sr_n = make_int2(0, 0);
   int o_n = 0, e_n = 0;
   if (AHEAD && s < S) { sr_n = srows[s]; o_n = off[s]; e_n = off[s + 1]; }
+#if GBILU_SPMV_PREFETCH > 0
+  // the first rounds of this warp's slices asked from L2 here (lane k:
+  // round k), then the slice GBILU_SPMV_PREFETCH rounds ahead of each
+  if (PF && lane < GBILU_SPMV_PREFETCH && s + lane * nwarps < S) {
+    const int sp = s + lane * nwarps, po = off[sp];
+    prefetch_slice<V>(sp, po, off[sp + 1] - po, col, val, val, false);
+  }
+#endif
   for (; s < S; s += nwarps) {
+#if GBILU_SPMV_PREFETCH > 0
+    const int sp = s + GBILU_SPMV_PREFETCH * nwarps;
+    const int po = PF && lane == 0 && sp < S ? off[sp] : 0;
+    const int pe = PF && lane == 0 && sp < S ? off[sp + 1] : 0;
+#endif
     int2 sr;
     int o, wdt;
     if (AHEAD) {
@@ -399,6 +451,9 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
         }
       }
     }
+#if GBILU_SPMV_PREFETCH > 0
+    if (PF && lane == 0 && sp < S) prefetch_slice<V>(sp, po, pe - po, col, val, val, false);
+#endif
   }
   if (MODE == SPMV_PLAIN) return;
   if (sizeof(T) == 4) { d1 = df_value(f1); d2 = df_value(f2); }
@@ -890,6 +945,24 @@ __device__ __forceinline__ void group_sync(int g) {
 #ifndef GBILU_LARGE_CACHED
 #define GBILU_LARGE_CACHED 1
 #endif
+#ifndef GBILU_DYNAMIC_LARGE
+#define GBILU_DYNAMIC_LARGE 1
+#endif
+#ifndef GBILU_DYN_MIN_ROUNDS
+#define GBILU_DYN_MIN_ROUNDS 1LL
+#endif
+#ifndef GBILU_DYN_FIRST_STATIC
+#define GBILU_DYN_FIRST_STATIC 1
+#endif
+#ifndef GBILU_DYN_MAX_ROUNDS
+#define GBILU_DYN_MAX_ROUNDS (1LL << 30)
+#endif
+// Large steps: each warp asks L2 for the matrix slice it (or, with the
+// dynamic order, another warp) will take this many rounds of the grid's
+// warps ahead, by one bulk prefetch per array; 0 turns it off.
+#ifndef GBILU_L2_PREFETCH
+#define GBILU_L2_PREFETCH 0
+#endif
 // Vector loads of the large steps go through L1. Every large step follows a
 // grid barrier whose acquire (ld.acquire.gpu, then the CTA barrier) orders
 // the earlier steps' writes from other SMs before these loads, and no row a
@@ -1115,6 +1188,11 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
         for (int k = 0; k < 3; ++k) st_relaxed(hat + 3 * row + k, sent);
     }
   }
+  // the slice counters of the large steps after the first: cleared here,
+  // before this CTA's first grid barrier, so before any of those steps
+  // starts; the first step keeps the static assignment
+  if (GBILU_DYNAMIC_LARGE && blockIdx.x == 0 && threadIdx.x < ph.n && threadIdx.x > 0)
+    ctl->step_next[threadIdx.x] = 0u;
   unsigned char *ring_base = stage_smem + sp.ring_off;
   if (ring && warp == NT / 32 - 1) {
     // the producer warp (one lane per stage) leaves the CTA's barriers
@@ -1260,15 +1338,59 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
       }
       gseq += nq;
     } else {
-      // slice j of the step goes to CTA j % grid: the device numbering puts
-      // a color's widest rows first, and contiguous chunks per CTA would
-      // hand them all to the first CTAs, which every barrier then waits for
       const int nsl = (P.nrows + 31) >> 5;
-      for (int j = warp * gridDim.x + blockIdx.x; j < nsl; j += stride >> 5) {
+      // Warp w of CTA b first takes slice w * grid + b (one round of the
+      // grid's warps; slice j lands on CTA j % grid: the device numbering
+      // puts a color's widest rows first, and contiguous chunks per CTA
+      // would hand them all to the first CTAs, which every barrier then
+      // waits for). Static: every further round the same way. dyn: the
+      // slices after the first round are handed out in order by a counter,
+      // so a warp that drew narrow slices takes more, each warp fetching
+      // its next while it computes the current one. Only for steps after
+      // the first with more slices than the grid has warps: a grid barrier
+      // precedes each of them, CTA 0 cleared the counter before its first
+      // grid barrier, and the one-slice steps that a CTA barrier links to a
+      // neighbouring step keep their static owner.
+      const long long nwt = stride >> 5;
+      const bool dyn = GBILU_DYNAMIC_LARGE && q > 0 && nsl > 1 &&
+                       nsl > GBILU_DYN_MIN_ROUNDS * nwt && nsl <= GBILU_DYN_MAX_ROUNDS * nwt;
+      unsigned int *ctr = &ctl->step_next[q];
+#if GBILU_L2_PREFETCH > 0
+      // the first rounds here (lane k: round k of this warp's static
+      // order), then round + GBILU_L2_PREFETCH of each slice taken
+      const int nw = stride >> 5;
+      const bool pd = P.uses_d();
+      constexpr bool PF = sizeof(V) == 4;   // the FP64 steps are bound by the FP64 unit
+      if (PF && lane < GBILU_L2_PREFETCH) {
+        const int jp = warp * (int)gridDim.x + (int)blockIdx.x + lane * nw;
+        if (jp < nsl) {
+          const int o = off[P.slice0 + jp];
+          prefetch_slice<V>(P.slice0 + jp, o, off[P.slice0 + jp + 1] - o, col, val, dmat, pd);
+        }
+      }
+#endif
+      int j = GBILU_DYN_FIRST_STATIC || !dyn
+                  ? warp * (int)gridDim.x + (int)blockIdx.x
+                  : __shfl_sync(0xffffffffu, lane == 0 ? (int)atomicAdd(ctr, 1u) : 0, 0);
+      const int first_dyn = GBILU_DYN_FIRST_STATIC ? (int)nwt : 0;
+      while (j < nsl) {
+        const int jn =
+            dyn ? (lane == 0 ? first_dyn + (int)atomicAdd(ctr, 1u) : 0) : j + (stride >> 5);
+#if GBILU_L2_PREFETCH > 0
+        // loaded now, the prefetch issued after this slice's row
+        const int jp = j + GBILU_L2_PREFETCH * nw;
+        const int po = PF && lane == 0 && jp < nsl ? off[P.slice0 + jp] : 0;
+        const int pe = PF && lane == 0 && jp < nsl ? off[P.slice0 + jp + 1] : 0;
+#endif
         const int t = 32 * j + lane;
         if (t < P.nrows)
           phase_row<V, T, !kLargeCached>(P, P.row0 + t, P.slice0 + j, lane, off, col, val, dmat,
                                          src, ybuf, hat);
+#if GBILU_L2_PREFETCH > 0
+        if (PF && lane == 0 && jp < nsl)
+          prefetch_slice<V>(P.slice0 + jp, po, pe - po, col, val, dmat, pd);
+#endif
+        j = dyn ? __shfl_sync(0xffffffffu, jn, 0) : jn;
       }
     }
     bool ok = true;
