@@ -306,8 +306,9 @@ template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p) {
 // w blocks costs about 2*ceil(w/kBatch) memory round trips instead of 2*w.
 // Padding slots (column -1) only occur after a row's last block.
 // Neighbour columns below lo are read from xlo instead of x (the first sweep
-// reads the input vector for color 0, whose L rows are empty).
-template <typename V, typename T, bool NEG, bool CG>
+// reads the input vector for color 0, whose L rows are empty). EARLY: the
+// block values are loaded without waiting for the column indices.
+template <typename V, typename T, bool NEG, bool CG, bool EARLY>
 __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V *__restrict__ val,
                                            int o, int wdt, int lane, const T *x, const T *xlo,
                                            int lo, T &a0, T &a1, T &a2) {
@@ -319,18 +320,28 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
 #pragma unroll
     for (int j = 0; j < B; ++j)
       c[j] = (k0 + j < wdt) ? ldg_stream(col + (size_t)(o + k0 + j) * 32 + lane) : -1;
-    // all loads of the batch first ...
+    // all loads of the batch first ... The values of every slot of the
+    // slice exist for all 32 lanes (padding: zeros, column -1), so with
+    // EARLY they are loaded whatever the column index says and go out
+    // together with the index loads instead of after them; only the
+    // gathers wait for the index.
     T xv[B][3];
     V b[B][9];
 #pragma unroll
     for (int j = 0; j < B; ++j) {
+      const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
+      if (EARLY && k0 + j < wdt) {
+#pragma unroll
+        for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
+      }
       if (c[j] >= 0) {
-        const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
         const T *xs = c[j] < lo ? xlo : x;
 #pragma unroll
         for (int e = 0; e < 3; ++e) xv[j][e] = ldv<CG>(xs + 3 * c[j] + e);
+        if (!EARLY) {
 #pragma unroll
-        for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
+          for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
+        }
       }
     }
     // ... then the multiply-adds
@@ -399,6 +410,9 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
   // solve gains 1.5 %). FP64 is bound by the FP64 unit, and the extra
   // registers spill in its dot modes: it loads them per slice.
   constexpr bool AHEAD = sizeof(V) == 4;
+  // values loaded ahead of the column indices in FP32; the FP64 SpMV with
+  // fused dots ran 1-3 % slower that way (FP64 unit bound)
+  constexpr bool kSpmvEarly = sizeof(V) == 4;
   // FP32 matrices only: the FP64 SpMV is bound by the FP64 unit
   constexpr bool PF = sizeof(V) == 4;
   int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
@@ -432,7 +446,7 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
     if (lane < sr.y) {
       const int row = sr.x + lane;
       T a0 = 0, a1 = 0, a2 = 0;
-      row_blocks<V, T, false, false>(col, val, o, wdt, lane, x, x, 0, a0, a1, a2);
+      row_blocks<V, T, false, false, kSpmvEarly>(col, val, o, wdt, lane, x, x, 0, a0, a1, a2);
       if (RES) {
         a0 = w[3 * row] - a0; a1 = w[3 * row + 1] - a1; a2 = w[3 * row + 2] - a2;
       }
@@ -552,6 +566,9 @@ __device__ __forceinline__ void phase_store(const Phase &P, int row, const V *d,
   hat[3 * row] = a0; hat[3 * row + 1] = a1; hat[3 * row + 2] = a2;
 }
 
+#ifndef GBILU_D_PREFETCH
+#define GBILU_D_PREFETCH 1
+#endif
 // One row of a step, one thread: a = own_i - sum_j B_ij nbr_j, then stored.
 template <typename V, typename T, bool CG>
 __device__ __forceinline__ void phase_row(const Phase &P, int row, int s, int lane,
@@ -559,9 +576,17 @@ __device__ __forceinline__ void phase_row(const Phase &P, int row, int s, int la
                                           const V *__restrict__ val, const V *__restrict__ dmat,
                                           const T *src, T *ybuf, T *hat) {
   const T *own = P.own_y ? ybuf : src;
+  if (GBILU_D_PREFETCH && (P.has_d || (P.to_y && P.final_d && row - lane + 31 >= P.final0))) {
+    // the slice's D block (9 * 32 values, one 128-byte line per lane) is
+    // read at the end of the row: asked from L2 now, without registers
+    constexpr int kLines = 9 * 32 * (int)sizeof(V) / 128;
+    if (lane < kLines)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(dmat + (size_t)s * 9 * 32 +
+                                                     lane * (128 / (int)sizeof(V))));
+  }
   const int o = off[s], wdt = off[s + 1] - o;
   T a0 = ldv<CG>(own + 3 * row), a1 = ldv<CG>(own + 3 * row + 1), a2 = ldv<CG>(own + 3 * row + 2);
-  row_blocks<V, T, true, CG>(col, val, o, wdt, lane, P.nbr_hat ? hat : ybuf, src, P.src_rows, a0,
+  row_blocks<V, T, true, CG, true>(col, val, o, wdt, lane, P.nbr_hat ? hat : ybuf, src, P.src_rows, a0,
                              a1, a2);
   phase_store<V, T, true>(P, row, dmat + (size_t)s * 9 * 32 + lane, a0, a1, a2, ybuf, hat);
 }
