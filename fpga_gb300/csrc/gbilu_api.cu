@@ -644,14 +644,24 @@ int upload_mat(Handle *h, const SlicedMatrix &m, DevMat &d) {
   return GBILU_OK;
 }
 
+// FP32 copy of an FP64 sliced value array (slots of 9 x 32 entries), in the
+// FP32 layout (sl_idx).
+std::vector<float> to_sliced32(const std::vector<double> &v64, size_t slots) {
+  std::vector<float> t32(v64.size());
+  for (size_t slot = 0; slot < slots; ++slot)
+    for (int e = 0; e < 9; ++e)
+      for (int l = 0; l < kSliceRows; ++l)
+        t32[sl_idx<float>(slot, e, l)] = (float)v64[sl_idx<double>(slot, e, l)];
+  return t32;
+}
+
 int upload_vals(Handle *h, const SlicedMatrix &m, const double *src, DevMat &d) {
   const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
   std::vector<double> tmp(nv);
   fill_sliced<double>(m, src, tmp.data());
   CK(cudaMemcpy(d.v64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
-    std::vector<float> t32(nv);
-    for (size_t i = 0; i < nv; ++i) t32[i] = (float)tmp[i];
+    const std::vector<float> t32 = to_sliced32(tmp, (size_t)m.slots());
     CK(cudaMemcpy(d.v32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
   }
   return GBILU_OK;
@@ -663,8 +673,7 @@ int upload_diag(Handle *h, bool transpose, DevBuf<double> &d64, DevBuf<float> &d
   fill_sliced_diag<double>(h->an, h->dinv.data(), transpose, tmp.data());
   CK(cudaMemcpy(d64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
-    std::vector<float> t32(nv);
-    for (size_t i = 0; i < nv; ++i) t32[i] = (float)tmp[i];
+    const std::vector<float> t32 = to_sliced32(tmp, (size_t)h->an.S);
     CK(cudaMemcpy(d32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
   }
   return GBILU_OK;

@@ -445,8 +445,6 @@ void fill_sliced_diag(const Analysis &an, const double *d, bool transpose, V *ou
 }
 
 template void fill_sliced<double>(const SlicedMatrix &, const double *, double *);
-template void fill_sliced<float>(const SlicedMatrix &, const double *, float *);
 template void fill_sliced_diag<double>(const Analysis &, const double *, bool, double *);
-template void fill_sliced_diag<float>(const Analysis &, const double *, bool, float *);
 
 }  // namespace gbilu

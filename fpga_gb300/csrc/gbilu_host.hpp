@@ -21,7 +21,9 @@ constexpr int kSliceRows = 32;  // block rows per slice = one warp
 // slice_row0[s] + slice_len[s] - 1 of one color; row lane l of slice s keeps
 // its k-th block in slot off[s] + k: column col[slot*32 + l] (a device row;
 // -1 = padding, always after the row's last block) and value entry e at
-// val[(slot*9 + e)*32 + l]. Blocks of a row are in ascending column order of
+// val[(slot*9 + e)*32 + l] in FP64 (FP32 copies: entries 0-3 and 4-7 as 4
+// consecutive floats per lane, entry 8 one float per lane, within the same
+// 288 values of the slot). Blocks of a row are in ascending column order of
 // the permuted numbering.
 struct SlicedMatrix {
   std::vector<int> off;   // [S+1]
@@ -100,13 +102,17 @@ int bilu0(const Analysis &an, double *pvals, double *dinv);
 // Gathers input-order values into the permuted order.
 void permute_values(const Analysis &an, const double *vals, double *pvals);
 
-// Fills a sliced value array (slots*9*32 entries of type V) from a value
-// source array (9 doubles per block); padding entries become 0.
+// Fills an FP64 sliced value array (slots*9*32 entries, the FP64 layout
+// [(slot*9 + e)*32 + l]) from a value source array (9 doubles per block);
+// padding entries become 0. The FP32 copies on the device use the FP32
+// layout of the kernels (two 16-byte groups and one float per lane and
+// slot), converted from this one.
 template <typename V>
 void fill_sliced(const SlicedMatrix &m, const double *src, V *out);
 
 // Sliced copy of per-row 3x3 blocks (nb*9 doubles in permuted row order),
-// optionally transposed, laid out [(slice*9 + e)*32 + lane] by device row.
+// optionally transposed, laid out [(slice*9 + e)*32 + lane] by device row
+// (FP64 layout, as fill_sliced).
 template <typename V>
 void fill_sliced_diag(const Analysis &an, const double *dinv, bool transpose,
                       V *out);

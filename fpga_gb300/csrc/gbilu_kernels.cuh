@@ -65,6 +65,38 @@ struct Ctl {
 
 template <typename T> __device__ __forceinline__ T ldg_stream(const T *p) { return __ldcs(p); }
 
+// Entry e (row-major in the 3x3 block) of lane l in slot `slot` of a sliced
+// value array of V; the D^-1 arrays use the same layout with one slot per
+// slice. FP64: [(slot*9 + e)*32 + l], entry-major, each of a warp's 9 loads
+// one coalesced 256-byte access. FP32: the slot's 288 values in three groups,
+// entries 0-3 and 4-7 with their 4 floats consecutive per lane and entry 8
+// with one float per lane, so that a lane reads its block with two 16-byte
+// loads and one 4-byte load instead of nine (each warp load still one
+// contiguous range): the FP32 SpMV and sweeps wait less on the load queue.
+template <typename V> __host__ __device__ inline size_t sl_idx(size_t slot, int e, int l) {
+  if (sizeof(V) == 4)
+    return slot * 288 + (e < 8 ? (size_t)(e >> 2) * 128 + (size_t)l * 4 + (size_t)(e & 3)
+                               : 256 + (size_t)l);
+  return (slot * 9 + (size_t)e) * 32 + (size_t)l;
+}
+
+// The 9 entries of lane l's block in the slot that starts at b, from global
+// memory (streaming loads) or from shared memory.
+template <typename V, bool GLOBAL>
+__device__ __forceinline__ void load_block(const V *b, int l, V (&e)[9]) {
+  if constexpr (sizeof(V) == 4) {
+    const float4 *q = reinterpret_cast<const float4 *>(b);
+    const float4 u = GLOBAL ? __ldcs(q + l) : q[l];
+    const float4 w = GLOBAL ? __ldcs(q + 32 + l) : q[32 + l];
+    e[0] = u.x; e[1] = u.y; e[2] = u.z; e[3] = u.w;
+    e[4] = w.x; e[5] = w.y; e[6] = w.z; e[7] = w.w;
+    e[8] = GLOBAL ? __ldcs(b + 256 + l) : b[256 + l];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) e[k] = GLOBAL ? __ldcs(b + k * 32 + l) : b[k * 32 + l];
+  }
+}
+
 // L2 prefetch of matrix slices ahead of the warp that will read them (the
 // large steps of the single-launch apply, the SpMV): rounds of the grid's
 // warps ahead; 0 turns it off.
@@ -329,19 +361,13 @@ __device__ __forceinline__ void row_blocks(const int *__restrict__ col, const V 
     V b[B][9];
 #pragma unroll
     for (int j = 0; j < B; ++j) {
-      const V *v = val + (size_t)(o + k0 + j) * 9 * 32 + lane;
-      if (EARLY && k0 + j < wdt) {
-#pragma unroll
-        for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
-      }
+      const V *v = val + (size_t)(o + k0 + j) * 9 * 32;   // the slot
+      if (EARLY && k0 + j < wdt) load_block<V, true>(v, lane, b[j]);
       if (c[j] >= 0) {
         const T *xs = c[j] < lo ? xlo : x;
 #pragma unroll
         for (int e = 0; e < 3; ++e) xv[j][e] = ldv<CG>(xs + 3 * c[j] + e);
-        if (!EARLY) {
-#pragma unroll
-          for (int e = 0; e < 9; ++e) b[j][e] = ldg_stream(v + e * 32);
-        }
+        if (!EARLY) load_block<V, true>(v, lane, b[j]);
       }
     }
     // ... then the multiply-adds
@@ -413,8 +439,10 @@ k_spmv(Ctl *ctl, int S, const int2 *__restrict__ srows, const int *__restrict__ 
   // values loaded ahead of the column indices in FP32; the FP64 SpMV with
   // fused dots ran 1-3 % slower that way (FP64 unit bound)
   constexpr bool kSpmvEarly = sizeof(V) == 4;
+#if GBILU_SPMV_PREFETCH > 0
   // FP32 matrices only: the FP64 SpMV is bound by the FP64 unit
   constexpr bool PF = sizeof(V) == 4;
+#endif
   int s = blockIdx.x * kWarps + (threadIdx.x >> 5);
   int2 sr_n = make_int2(0, 0);
   int o_n = 0, e_n = 0;
@@ -541,27 +569,30 @@ __device__ __forceinline__ T dot3(T d0, T d1, T d2, T a0, T a1, T a2) {
   return fma(d2, a2, fma(d1, a1, d0 * a0));
 }
 
-// (a0, a1, a2) <- D (a0, a1, a2) with D at d[e*32], e = 0..8 (row-major)
+// (a0, a1, a2) <- D (a0, a1, a2) with D lane l's block of the slot at d
 template <typename V, typename T, bool GLOBAL>
-__device__ __forceinline__ void apply_dp(const V *d, T &a0, T &a1, T &a2) {
+__device__ __forceinline__ void apply_dp(const V *d, int l, T &a0, T &a1, T &a2) {
+  V dv[9];
+  load_block<V, GLOBAL>(d, l, dv);
   T dd[9];
 #pragma unroll
-  for (int e = 0; e < 9; ++e) dd[e] = GLOBAL ? (T)ldg_stream(d + e * 32) : (T)d[e * 32];
+  for (int e = 0; e < 9; ++e) dd[e] = (T)dv[e];
   const T z0 = dot3(dd[0], dd[1], dd[2], a0, a1, a2);
   const T z1 = dot3(dd[3], dd[4], dd[5], a0, a1, a2);
   const T z2 = dot3(dd[6], dd[7], dd[8], a0, a1, a2);
   a0 = z0; a1 = z1; a2 = z2;
 }
 
-// Stores one row's result as the phase says (d: this row's D block).
+// Stores one row's result as the phase says (d: the slot of the row's D
+// block, l: the row's lane).
 template <typename V, typename T, bool GLOBAL>
-__device__ __forceinline__ void phase_store(const Phase &P, int row, const V *d, T a0, T a1,
-                                            T a2, T *ybuf, T *hat) {
-  if (P.has_d) apply_dp<V, T, GLOBAL>(d, a0, a1, a2);
+__device__ __forceinline__ void phase_store(const Phase &P, int row, const V *d, int l, T a0,
+                                            T a1, T a2, T *ybuf, T *hat) {
+  if (P.has_d) apply_dp<V, T, GLOBAL>(d, l, a0, a1, a2);
   if (P.to_y) {
     ybuf[3 * row] = a0; ybuf[3 * row + 1] = a1; ybuf[3 * row + 2] = a2;
     if (row < P.final0) return;
-    if (P.final_d) apply_dp<V, T, GLOBAL>(d, a0, a1, a2);
+    if (P.final_d) apply_dp<V, T, GLOBAL>(d, l, a0, a1, a2);
   }
   hat[3 * row] = a0; hat[3 * row + 1] = a1; hat[3 * row + 2] = a2;
 }
@@ -588,7 +619,7 @@ __device__ __forceinline__ void phase_row(const Phase &P, int row, int s, int la
   T a0 = ldv<CG>(own + 3 * row), a1 = ldv<CG>(own + 3 * row + 1), a2 = ldv<CG>(own + 3 * row + 2);
   row_blocks<V, T, true, CG, true>(col, val, o, wdt, lane, P.nbr_hat ? hat : ybuf, src, P.src_rows, a0,
                              a1, a2);
-  phase_store<V, T, true>(P, row, dmat + (size_t)s * 9 * 32 + lane, a0, a1, a2, ybuf, hat);
+  phase_store<V, T, true>(P, row, dmat + (size_t)s * 9 * 32, lane, a0, a1, a2, ybuf, hat);
 }
 
 // Colors with at most kSmallRows rows cannot fill the GPU: their steps are
@@ -888,21 +919,22 @@ __device__ __forceinline__ void staged_row(const Phase &P, int row, int lane, in
 #pragma unroll
     for (int j = 0; j < SB; ++j)
       if (c[j] >= 0) {
-        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + lane;
-        a0 = fma(-(T)b[0 * 32], y[j][0], a0); a0 = fma(-(T)b[1 * 32], y[j][1], a0);
-        a0 = fma(-(T)b[2 * 32], y[j][2], a0);
-        a1 = fma(-(T)b[3 * 32], y[j][0], a1); a1 = fma(-(T)b[4 * 32], y[j][1], a1);
-        a1 = fma(-(T)b[5 * 32], y[j][2], a1);
-        a2 = fma(-(T)b[6 * 32], y[j][0], a2); a2 = fma(-(T)b[7 * 32], y[j][1], a2);
-        a2 = fma(-(T)b[8 * 32], y[j][2], a2);
+        V b[9];
+        load_block<V, false>(sv + (size_t)(k0 + j) * 9 * 32, lane, b);
+        a0 = fma(-(T)b[0], y[j][0], a0); a0 = fma(-(T)b[1], y[j][1], a0);
+        a0 = fma(-(T)b[2], y[j][2], a0);
+        a1 = fma(-(T)b[3], y[j][0], a1); a1 = fma(-(T)b[4], y[j][1], a1);
+        a1 = fma(-(T)b[5], y[j][2], a1);
+        a2 = fma(-(T)b[6], y[j][0], a2); a2 = fma(-(T)b[7], y[j][1], a2);
+        a2 = fma(-(T)b[8], y[j][2], a2);
       }
   }
-  if (P.has_d) apply_dp<V, T, false>(sd + lane, a0, a1, a2);
+  if (P.has_d) apply_dp<V, T, false>(sd, lane, a0, a1, a2);
   if (P.to_y) {
     st_relaxed(ybuf + 3 * row, a0); st_relaxed(ybuf + 3 * row + 1, a1);
     st_relaxed(ybuf + 3 * row + 2, a2);
     if (row < P.final0) return;
-    if (P.final_d) apply_dp<V, T, false>(sd + lane, a0, a1, a2);
+    if (P.final_d) apply_dp<V, T, false>(sd, lane, a0, a1, a2);
   }
   st_relaxed(hat + 3 * row, a0); st_relaxed(hat + 3 * row + 1, a1); st_relaxed(hat + 3 * row + 2, a2);
 }
@@ -946,10 +978,10 @@ __device__ __forceinline__ T staged_comp(const Phase &P, int c, int row, int lan
 #pragma unroll
     for (int j = 0; j < SB; ++j)
       if (cc[j] >= 0) {
-        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + 3 * c * 32 + lane;
-        a = fma(-(T)b[0], y[j][0], a);
-        a = fma(-(T)b[32], y[j][1], a);
-        a = fma(-(T)b[64], y[j][2], a);
+        const V *b = sv + (size_t)(k0 + j) * 9 * 32;
+        a = fma(-(T)b[sl_idx<V>(0, 3 * c, lane)], y[j][0], a);
+        a = fma(-(T)b[sl_idx<V>(0, 3 * c + 1, lane)], y[j][1], a);
+        a = fma(-(T)b[sl_idx<V>(0, 3 * c + 2, lane)], y[j][2], a);
       }
   }
   return a;
@@ -1122,16 +1154,17 @@ __device__ __forceinline__ void ring_row(const Phase &P, int row, int lane, int 
 #pragma unroll
     for (int j = 0; j < B; ++j)
       if (c[j] >= 0) {
-        const V *b = sv + (size_t)(k0 + j) * 9 * 32 + lane;
-        a0 = fma(-(T)b[0 * 32], x[j][0], a0); a0 = fma(-(T)b[1 * 32], x[j][1], a0);
-        a0 = fma(-(T)b[2 * 32], x[j][2], a0);
-        a1 = fma(-(T)b[3 * 32], x[j][0], a1); a1 = fma(-(T)b[4 * 32], x[j][1], a1);
-        a1 = fma(-(T)b[5 * 32], x[j][2], a1);
-        a2 = fma(-(T)b[6 * 32], x[j][0], a2); a2 = fma(-(T)b[7 * 32], x[j][1], a2);
-        a2 = fma(-(T)b[8 * 32], x[j][2], a2);
+        V b[9];
+        load_block<V, false>(sv + (size_t)(k0 + j) * 9 * 32, lane, b);
+        a0 = fma(-(T)b[0], x[j][0], a0); a0 = fma(-(T)b[1], x[j][1], a0);
+        a0 = fma(-(T)b[2], x[j][2], a0);
+        a1 = fma(-(T)b[3], x[j][0], a1); a1 = fma(-(T)b[4], x[j][1], a1);
+        a1 = fma(-(T)b[5], x[j][2], a1);
+        a2 = fma(-(T)b[6], x[j][0], a2); a2 = fma(-(T)b[7], x[j][1], a2);
+        a2 = fma(-(T)b[8], x[j][2], a2);
       }
   }
-  phase_store<V, T, false>(P, row, sd + lane, a0, a1, a2, ybuf, hat);
+  phase_store<V, T, false>(P, row, sd, lane, a0, a1, a2, ybuf, hat);
 }
 
 // hat = M^-1 src (or M^-T src): all color steps of the L and U sweeps in one
@@ -1286,7 +1319,7 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
             const int *sc =
                 reinterpret_cast<const int *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V));
             sd = reinterpret_cast<const V *>(stage_smem + E.pos + E.w * 9 * 32 * sizeof(V) +
-                                             E.w * 32 * sizeof(int)) + lane;
+                                             E.w * 32 * sizeof(int));
             if (valid) a = staged_comp<V, T>(P, c, row, lane, E.w, sv, sc, src, ybuf, hat, ctl);
           }
           if (!act) continue;   // the whole group (same e) skips the round
@@ -1297,8 +1330,9 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
             xch[grp][c][lane] = a;
             group_sync(grp);
             if (valid)
-              a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
-                          xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
+              a = dot3<T>((T)sd[sl_idx<V>(0, 3 * c, lane)], (T)sd[sl_idx<V>(0, 3 * c + 1, lane)],
+                          (T)sd[sl_idx<V>(0, 3 * c + 2, lane)], xch[grp][0][lane],
+                          xch[grp][1][lane], xch[grp][2][lane]);
             group_sync(grp);
           }
           bool fin = true;
@@ -1309,8 +1343,9 @@ k_ilu_coop(Ctl *ctl, PhaseList ph, StagePlan sp, const int *__restrict__ off1,
               xch[grp][c][lane] = a;
               group_sync(grp);
               if (valid && fin)
-                a = dot3<T>((T)sd[3 * c * 32], (T)sd[(3 * c + 1) * 32], (T)sd[(3 * c + 2) * 32],
-                            xch[grp][0][lane], xch[grp][1][lane], xch[grp][2][lane]);
+                a = dot3<T>((T)sd[sl_idx<V>(0, 3 * c, lane)], (T)sd[sl_idx<V>(0, 3 * c + 1, lane)],
+                            (T)sd[sl_idx<V>(0, 3 * c + 2, lane)], xch[grp][0][lane],
+                            xch[grp][1][lane], xch[grp][2][lane]);
               group_sync(grp);
             }
           }
@@ -1926,12 +1961,12 @@ __global__ void k_fill_sliced(long long slots, const int *__restrict__ vsrc, int
     for (int e = 0; e < 9; ++e) {
       const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
       const double x = sblk >= 0 ? src[(size_t)sblk * 9 + ee] : 0.0;
-      out[(slot * 9 + e) * 32 + lane] = (V)x;
+      out[sl_idx<V>((size_t)slot, e, lane)] = (V)x;
     }
   }
 }
 
-// Sliced per-row 3x3 blocks [(s*9 + e)*32 + lane] from nb*9 doubles in
+// Sliced per-row 3x3 blocks (sl_idx, one slot per slice) from nb*9 doubles in
 // permuted row order (drow: device row -> permuted row).
 template <typename V>
 __global__ void k_fill_diag(int S, const int2 *__restrict__ srows, const int *__restrict__ drow,
@@ -1944,7 +1979,7 @@ __global__ void k_fill_diag(int S, const int2 *__restrict__ srows, const int *__
     for (int e = 0; e < 9; ++e) {
       const int ee = transpose ? (e % 3) * 3 + e / 3 : e;
       const double x = lane < sr.y ? d[(size_t)drow[sr.x + lane] * 9 + ee] : 0.0;
-      out[((size_t)s * 9 + e) * 32 + lane] = (V)x;
+      out[sl_idx<V>((size_t)s, e, lane)] = (V)x;
     }
   }
 }
