@@ -644,24 +644,26 @@ int upload_mat(Handle *h, const SlicedMatrix &m, DevMat &d) {
   return GBILU_OK;
 }
 
-// FP32 copy of an FP64 sliced value array (slots of 9 x 32 entries), in the
-// FP32 layout (sl_idx).
-std::vector<float> to_sliced32(const std::vector<double> &v64, size_t slots) {
-  std::vector<float> t32(v64.size());
+// A sliced value array of the host fill (FP64, entry-major: slots of
+// [(slot*9 + e)*32 + l]) in the device layout of V (sl_idx).
+template <typename V>
+std::vector<V> to_device_layout(const std::vector<double> &em, size_t slots) {
+  std::vector<V> out(em.size());
   for (size_t slot = 0; slot < slots; ++slot)
     for (int e = 0; e < 9; ++e)
       for (int l = 0; l < kSliceRows; ++l)
-        t32[sl_idx<float>(slot, e, l)] = (float)v64[sl_idx<double>(slot, e, l)];
-  return t32;
+        out[sl_idx<V>(slot, e, l)] = (V)em[(slot * 9 + e) * kSliceRows + l];
+  return out;
 }
 
 int upload_vals(Handle *h, const SlicedMatrix &m, const double *src, DevMat &d) {
   const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
   std::vector<double> tmp(nv);
   fill_sliced<double>(m, src, tmp.data());
-  CK(cudaMemcpy(d.v64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  const std::vector<double> t64 = to_device_layout<double>(tmp, (size_t)m.slots());
+  CK(cudaMemcpy(d.v64.p, t64.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
-    const std::vector<float> t32 = to_sliced32(tmp, (size_t)m.slots());
+    const std::vector<float> t32 = to_device_layout<float>(tmp, (size_t)m.slots());
     CK(cudaMemcpy(d.v32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
   }
   return GBILU_OK;
@@ -671,9 +673,10 @@ int upload_diag(Handle *h, bool transpose, DevBuf<double> &d64, DevBuf<float> &d
   const size_t nv = (size_t)h->an.S * 9 * kSliceRows;
   std::vector<double> tmp(nv);
   fill_sliced_diag<double>(h->an, h->dinv.data(), transpose, tmp.data());
-  CK(cudaMemcpy(d64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  const std::vector<double> t64 = to_device_layout<double>(tmp, (size_t)h->an.S);
+  CK(cudaMemcpy(d64.p, t64.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
-    const std::vector<float> t32 = to_sliced32(tmp, (size_t)h->an.S);
+    const std::vector<float> t32 = to_device_layout<float>(tmp, (size_t)h->an.S);
     CK(cudaMemcpy(d32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
   }
   return GBILU_OK;
