@@ -645,7 +645,8 @@ int upload_mat(Handle *h, const SlicedMatrix &m, DevMat &d) {
 }
 
 // A sliced value array of the host fill (FP64, entry-major: slots of
-// [(slot*9 + e)*32 + l]) in the device layout of V (sl_idx).
+// [(slot*9 + e)*32 + l], which is the FP64 device layout) in the device
+// layout of V (sl_idx); used for the FP32 copies.
 template <typename V>
 std::vector<V> to_device_layout(const std::vector<double> &em, size_t slots) {
   std::vector<V> out(em.size());
@@ -659,9 +660,8 @@ std::vector<V> to_device_layout(const std::vector<double> &em, size_t slots) {
 int upload_vals(Handle *h, const SlicedMatrix &m, const double *src, DevMat &d) {
   const size_t nv = (size_t)m.slots() * 9 * kSliceRows;
   std::vector<double> tmp(nv);
-  fill_sliced<double>(m, src, tmp.data());
-  const std::vector<double> t64 = to_device_layout<double>(tmp, (size_t)m.slots());
-  CK(cudaMemcpy(d.v64.p, t64.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  fill_sliced<double>(m, src, tmp.data());   // the FP64 device layout already
+  CK(cudaMemcpy(d.v64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
     const std::vector<float> t32 = to_device_layout<float>(tmp, (size_t)m.slots());
     CK(cudaMemcpy(d.v32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
@@ -673,8 +673,7 @@ int upload_diag(Handle *h, bool transpose, DevBuf<double> &d64, DevBuf<float> &d
   const size_t nv = (size_t)h->an.S * 9 * kSliceRows;
   std::vector<double> tmp(nv);
   fill_sliced_diag<double>(h->an, h->dinv.data(), transpose, tmp.data());
-  const std::vector<double> t64 = to_device_layout<double>(tmp, (size_t)h->an.S);
-  CK(cudaMemcpy(d64.p, t64.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d64.p, tmp.data(), nv * sizeof(double), cudaMemcpyHostToDevice));
   if (h->with_32) {
     const std::vector<float> t32 = to_device_layout<float>(tmp, (size_t)h->an.S);
     CK(cudaMemcpy(d32.p, t32.data(), nv * sizeof(float), cudaMemcpyHostToDevice));
