@@ -94,6 +94,7 @@ struct Handle {
   // dperm: device row -> permuted row (the device factorization's layout);
   // pdev: permuted row -> device row (the gradient's gather of lambda)
   DevBuf<int> perm, iperm, fperm, dperm, pdev, prowptr, pcol, psrc;
+  DevBuf<int> ibrow, icol;                   // input pattern: block -> row, column
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
   DevBuf<float> dinv32, dinvT32;
@@ -702,7 +703,7 @@ void release_device(Handle *h) {
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
   h->srows.release(); h->perm.release(); h->iperm.release(); h->fperm.release(); h->dperm.release();
-  h->pdev.release();
+  h->pdev.release(); h->ibrow.release(); h->icol.release();
   h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
@@ -754,6 +755,15 @@ int setup_device(Handle *h) {
   CK(cudaMemcpy(h->dperm.p, an.dperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->pdev.alloc(an.nb));
   CK(cudaMemcpy(h->pdev.p, an.idperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> br(an.nnzb);
+    for (int i = 0; i < an.nb; ++i)
+      for (int k = an.rowptr[i]; k < an.rowptr[i + 1]; ++k) br[k] = i;
+    CK(h->ibrow.alloc(an.nnzb));
+    CK(cudaMemcpy(h->ibrow.p, br.data(), an.nnzb * sizeof(int), cudaMemcpyHostToDevice));
+    CK(h->icol.alloc(an.nnzb));
+    CK(cudaMemcpy(h->icol.p, an.colind.data(), an.nnzb * sizeof(int), cudaMemcpyHostToDevice));
+  }
   CK(h->prowptr.alloc(an.nb + 1));
   CK(cudaMemcpy(h->prowptr.p, an.prowptr.data(), (an.nb + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->pcol.alloc(an.nnzb));
@@ -808,7 +818,7 @@ int setup_device(Handle *h) {
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
-                     (size_t)an.nnzb * 8 + (size_t)an.nb * 24;
+                     (size_t)an.nnzb * 16 + (size_t)an.nb * 24;
   return GBILU_OK;
 }
 
@@ -1374,19 +1384,17 @@ static int solve_impl(Handle *h, const double *b, double *x, bool device_ptrs, b
                  overlap_b ? db : nullptr);
   if (rc) return rc;
   if (gx && gdA) {
-    // lambda from the device numbering and x from the input numbering into
-    // the permuted numbering of the pattern arrays, then dL/dA
+    // lambda from the device numbering into the input numbering (x comes
+    // in it), then dL/dA in the input block order
     const double *xin = gx;
     if (!device_ptrs) {   // b's staging buffer is free once the solve read it
       CK(cudaMemcpyAsync(h->io64.p, gx, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
       xin = h->io64.p;
     }
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->pdev.p, h->v64.x.p, h->v64.r.p, 1.0);
-    k_gather<double, double><<<g, kThreads, 0, h->st>>>(nb, h->fperm.p, xin, h->v64.s.p, 1.0);
-    k_grad_a<<<grid_for(h, nb), kThreads, 0, h->st>>>(nb, h->prowptr.p, h->pcol.p, h->psrc.p,
-                                                      h->v64.r.p, h->v64.s.p,
-                                                      device_ptrs ? gdA : h->dA.p);
-    launches += 3;
+    k_scatter<double><<<g, kThreads, 0, h->st>>>(nb, h->perm.p, h->v64.x.p, h->v64.r.p);
+    k_grad_a<<<grid_for(h, (long long)h->an.nnzb * 9), kThreads, 0, h->st>>>(
+        h->an.nnzb, h->ibrow.p, h->icol.p, h->v64.r.p, xin, device_ptrs ? gdA : h->dA.p);
+    launches += 2;
   }
   // x back to the caller's numbering. When the initial residual already met
   // the bound, v64.x still holds x0 (gathered), so this returns x0 unchanged

@@ -1833,21 +1833,23 @@ k_dot_check(Ctl *ctl, int n, const float *__restrict__ x, const float *__restric
   if (grid_sum<1>(v, partials, &ctl->counter[5], tot) && threadIdx.x == 0) ctl->dots[0] = tot[0];
 }
 
-// dA[src[k]] = -lambda_i x_j^T for the blocks k of permuted row i
-// (the pattern gradient of L(x(A)), x = A^-1 b).
-__global__ void k_grad_a(int nb, const int *__restrict__ prowptr, const int *__restrict__ pcol,
-                         const int *__restrict__ psrc, const double *__restrict__ lam,
-                         const double *__restrict__ x, double *__restrict__ dA) {
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < nb; i += gridDim.x * kThreads) {
-    const double l0 = lam[3 * i], l1 = lam[3 * i + 1], l2 = lam[3 * i + 2];
-    for (int k = prowptr[i]; k < prowptr[i + 1]; ++k) {
-      const int j = pcol[k];
-      const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-      double *o = dA + (size_t)psrc[k] * 9;
-      o[0] = -l0 * x0; o[1] = -l0 * x1; o[2] = -l0 * x2;
-      o[3] = -l1 * x0; o[4] = -l1 * x1; o[5] = -l1 * x2;
-      o[6] = -l2 * x0; o[7] = -l2 * x1; o[8] = -l2 * x2;
-    }
+// dA[b] = -lambda_i x_j^T for every block b = (i, j) of the pattern in the
+// input numbering and block order (the pattern gradient of L(x(A)),
+// x = A^-1 b; brow[b], col[b]: the block's row and column). One thread per
+// entry, in dA's order, so the 72 bytes written per block stream out in
+// order; lambda and x are read in the input numbering. (A thread per
+// permuted row spread each store over 32 cache lines, a warp per row waited
+// on a chain of dependent loads, a thread per entry of the permuted pattern
+// wrote scattered blocks: 1.44, 0.51 and 0.47 ms for the 2M-cell system.)
+__global__ void __launch_bounds__(kThreads)
+k_grad_a(long long nnzb, const int *__restrict__ brow, const int *__restrict__ col,
+         const double *__restrict__ lam, const double *__restrict__ x, double *__restrict__ dA) {
+  const long long n = 9 * nnzb;
+  for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < n;
+       t += (long long)gridDim.x * kThreads) {
+    const long long b = t / 9;
+    const int e = (int)(t - 9 * b);
+    dA[t] = -lam[3 * brow[b] + e / 3] * x[3 * col[b] + e % 3];
   }
 }
 
