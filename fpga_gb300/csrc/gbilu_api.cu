@@ -93,7 +93,7 @@ struct Handle {
   // fperm: permuted row -> input row (the pattern-ordered gradient);
   // dperm: device row -> permuted row (the device factorization's layout);
   // pdev: permuted row -> device row (the gradient's gather of lambda)
-  DevBuf<int> perm, iperm, fperm, dperm, pdev, prowptr, pcol, psrc;
+  DevBuf<int> perm, iperm, dperm, prowptr, pcol, psrc;
   DevBuf<int> ibrow, icol;                   // input pattern: block -> row, column
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
@@ -702,8 +702,8 @@ void release_device(Handle *h) {
     }
   h->pdiag.release(); h->bad.release(); h->pbuf.release(); h->vals_in.release();
   h->dinvp.release();
-  h->srows.release(); h->perm.release(); h->iperm.release(); h->fperm.release(); h->dperm.release();
-  h->pdev.release(); h->ibrow.release(); h->icol.release();
+  h->srows.release(); h->perm.release(); h->iperm.release(); h->dperm.release();
+  h->ibrow.release(); h->icol.release();
   h->prowptr.release(); h->pcol.release();
   h->psrc.release(); h->dinv64.release(); h->dinvT64.release(); h->dinv32.release();
   h->dinvT32.release(); h->v64.release(); h->v32.release(); h->b64.release();
@@ -749,12 +749,8 @@ int setup_device(Handle *h) {
     CK(h->iperm.alloc(an.nb));
     CK(cudaMemcpy(h->iperm.p, idv.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   }
-  CK(h->fperm.alloc(an.nb));
-  CK(cudaMemcpy(h->fperm.p, an.perm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   CK(h->dperm.alloc(an.nb));
   CK(cudaMemcpy(h->dperm.p, an.dperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
-  CK(h->pdev.alloc(an.nb));
-  CK(cudaMemcpy(h->pdev.p, an.idperm.data(), an.nb * sizeof(int), cudaMemcpyHostToDevice));
   {
     std::vector<int> br(an.nnzb);
     for (int i = 0; i < an.nb; ++i)
@@ -818,7 +814,7 @@ int setup_device(Handle *h) {
     }
   }
   h->device_bytes += nd * 16 + (h->with_32 ? nd * 8 : 0) + n * 8 * 12 + (h->with_32 ? n * 4 * 9 : 0) +
-                     (size_t)an.nnzb * 16 + (size_t)an.nb * 24;
+                     (size_t)an.nnzb * 16 + (size_t)an.nb * 16;
   return GBILU_OK;
 }
 
