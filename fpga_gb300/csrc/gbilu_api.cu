@@ -89,12 +89,11 @@ struct Handle {
   cudaStream_t aux = nullptr;
   cudaEvent_t e_x = nullptr, e_b = nullptr;
   DevBuf<int2> srows;
-  // perm/iperm: device row <-> input row (the vectors of a solve);
-  // fperm: permuted row -> input row (the pattern-ordered gradient);
-  // dperm: device row -> permuted row (the device factorization's layout);
-  // pdev: permuted row -> device row (the gradient's gather of lambda)
+  // perm/iperm: device row <-> input row (the vectors of a solve; lambda
+  // of the gradient); dperm: device row -> permuted row (the device
+  // factorization's layout); prowptr, pcol, psrc: the permuted pattern
   DevBuf<int> perm, iperm, dperm, prowptr, pcol, psrc;
-  DevBuf<int> ibrow, icol;                   // input pattern: block -> row, column
+  DevBuf<int> ibrow, icol;                   // input pattern: block -> row, column (dL/dA)
   DevMat A, L, U, At, Ut, Lt;
   DevBuf<double> dinv64, dinvT64;
   DevBuf<float> dinv32, dinvT32;
