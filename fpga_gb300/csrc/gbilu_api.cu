@@ -170,9 +170,12 @@ int grid_for(const Handle *h, long long work) {
 
 // Kernels that end in a grid reduction: fewer, fuller CTAs, so the
 // last-CTA step sees few partials and few serialized arrival atomics.
+#ifndef GBILU_REDUCE_CTAS_PER_SM
+#define GBILU_REDUCE_CTAS_PER_SM 2
+#endif
 int reduce_grid(const Handle *h, long long work) {
   long long g = (work + kThreads - 1) / kThreads;
-  const long long cap = (long long)h->sm_count * 2;
+  const long long cap = (long long)h->sm_count * GBILU_REDUCE_CTAS_PER_SM;
   return (int)std::max<long long>(1, std::min(g, cap));
 }
 
